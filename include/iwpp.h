@@ -1,0 +1,158 @@
+/*
+ * iwpp.h -- C ABI of the GB300 reconstruction-by-dilation library (libiwpp.so).
+ *
+ * Plain pointers and sizes only; `stream` is a cudaStream_t passed as void*
+ * (NULL = the legacy default stream).  Images are row-major with byte
+ * pitches and live in device memory unless stated otherwise.
+ *
+ * Semantics (all entry points): in place on `marker`, the result is the least
+ * image m >= marker with m[c] >= min(m[p], mask[c]) for every pair of
+ * neighbouring pixels p, c (4- or 8-connectivity; pixels outside the image do
+ * not exist).  With marker <= mask this is the grayscale reconstruction by
+ * dilation of marker under mask, the same bytes the reference computes
+ * (IWPP MP/src/MorphologicalReconstruction.cu:43-44 is the rule).
+ */
+#ifndef IWPP_H
+#define IWPP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IWPP_API __attribute__((visibility("default")))
+
+typedef enum iwpp_status {
+    IWPP_OK = 0,
+    IWPP_ERR_INVALID = 1,   /* bad argument */
+    IWPP_ERR_OOM = 2,       /* device allocation failed */
+    IWPP_ERR_TIMEOUT = 3,   /* a bounded device-side wait ran out */
+    IWPP_ERR_CUDA = 4,      /* a CUDA runtime call failed */
+    IWPP_ERR_OVERFLOW = 5,  /* queue overflowed more often than max_restarts */
+    IWPP_ERR_NO_DEVICE = 6, /* no CUDA device, or not a GB300-class (sm_103) one */
+    IWPP_ERR_BUSY = 7       /* a server is full or shutting down */
+} iwpp_status;
+
+typedef enum iwpp_dtype { IWPP_U8 = 0, IWPP_U16 = 1, IWPP_I32 = 2 } iwpp_dtype;
+
+/* The reference's three global-queue implementations (one per source
+ * directory).  Same result, different work queue. */
+typedef enum iwpp_queue_variant {
+    IWPP_QUEUE_DEFAULT = -1, /* IWPP_QUEUE_VARIANT env var, else UNIQUE */
+    IWPP_QUEUE_MUTEX = 0,    /* IWPP MP: LIFO stack under one spin mutex, one persistent launch */
+    IWPP_QUEUE_DOUBLE = 1,   /* IWPP MP DQ: read/write queues swapped every round */
+    IWPP_QUEUE_UNIQUE = 2    /* IWPP MP UQ: double queue, each tile at most once per round */
+} iwpp_queue_variant;
+
+typedef struct iwpp_config {
+    int tile_rows;             /* 32 or 64 rows per tile; 0 = default (autotuner table) */
+    long long queue_capacity;  /* entries per queue buffer; 0 = default */
+    int init_passes;           /* whole-image raster + anti-raster pairs first; -1 = default */
+    int grid_ctas;             /* persistent grid size; 0 = one full wave */
+    int max_restarts;          /* queue-overflow restarts allowed; 0 = default (64) */
+    int timeout_ms;            /* bound on every device-side wait; 0 = default (10000) */
+    int clip_marker;           /* 1: marker = min(marker, mask) before reconstructing */
+} iwpp_config;
+
+typedef struct iwpp_stats {
+    long long tiles;     /* tiles in the job */
+    long long visits;    /* tile visits (loads + local convergence) */
+    long long sweeps;    /* in-tile raster / anti-raster sweeps */
+    long long pushes;    /* queue insertions */
+    int rounds;          /* queue rounds (double / unique) */
+    int restarts;        /* overflow restarts from a full queue */
+    int status;          /* iwpp_status of the device run */
+    int variant;         /* queue variant used */
+    double device_ms;    /* device time of the reconstruction (events) */
+} iwpp_stats;
+
+/* One image of a batch. */
+typedef struct iwpp_image {
+    void *marker;
+    const void *mask;
+    size_t pitch_marker;
+    size_t pitch_mask;
+    int width;
+    int height;
+    int dtype;
+    int connectivity;
+} iwpp_image;
+
+typedef struct iwpp_handle_s *iwpp_handle;
+typedef struct iwpp_plan_s *iwpp_plan;
+
+/* ---- library ------------------------------------------------------------ */
+IWPP_API const char *iwpp_status_string(int status);
+IWPP_API int iwpp_version(void);
+/* Workspace owner (queues, tile states, counters) bound to one device.
+ * Calls that share a handle must be ordered on one stream. */
+IWPP_API int iwpp_handle_create(iwpp_handle *out, int device);
+IWPP_API int iwpp_handle_destroy(iwpp_handle h);
+/* Bytes of device workspace a job of `tiles` tiles needs. */
+IWPP_API long long iwpp_workspace_bytes(long long tiles, int variant, long long queue_capacity);
+/* Tiles of one image for a dtype and tile height (0 = default). */
+IWPP_API long long iwpp_tile_count(int width, int height, int dtype, int tile_rows);
+
+/* ---- plain reconstruction (replaces MorphologicalReconstruction,
+ *      IWPP MP/include/MorphologicalReconstruction.cuh:45-46, generalised to
+ *      any size, pitch, dtype, connectivity and queue variant) ------------- */
+IWPP_API int iwpp_reconstruct(iwpp_handle h, void *marker, const void *mask, size_t pitch_marker, size_t pitch_mask,
+                              int width, int height, int dtype, int connectivity, int variant,
+                              const iwpp_config *cfg, void *stream, iwpp_stats *stats);
+/* Same, asynchronous: enqueues on `stream` and returns; iwpp_handle_sync
+ * waits and reports the device status and counters of the last job. */
+IWPP_API int iwpp_reconstruct_async(iwpp_handle h, void *marker, const void *mask, size_t pitch_marker,
+                                    size_t pitch_mask, int width, int height, int dtype, int connectivity,
+                                    int variant, const iwpp_config *cfg, void *stream);
+IWPP_API int iwpp_handle_sync(iwpp_handle h, iwpp_stats *stats);
+
+/* ---- batched: all images in one persistent launch ----------------------- */
+IWPP_API int iwpp_reconstruct_batch(iwpp_handle h, const iwpp_image *images, int n, int variant,
+                                    const iwpp_config *cfg, void *stream, iwpp_stats *stats);
+/* A batch captured once into a CUDA graph (state reset + launches); every
+ * iwpp_plan_launch re-runs the reconstruction on the same buffers. */
+IWPP_API int iwpp_plan_create(iwpp_plan *out, iwpp_handle h, const iwpp_image *images, int n, int variant,
+                              const iwpp_config *cfg);
+IWPP_API int iwpp_plan_launch(iwpp_plan p, void *stream);
+IWPP_API int iwpp_plan_sync(iwpp_plan p, iwpp_stats *stats);
+IWPP_API int iwpp_plan_destroy(iwpp_plan p);
+
+/* ---- precondition helper (replaces the reference's clipImage kernel,
+ *      IWPP MP/src/MorphologicalReconstruction.cu:827-836) ----------------- */
+IWPP_API int iwpp_clip(void *marker, const void *mask, size_t pitch_marker, size_t pitch_mask, int width,
+                       int height, int dtype, void *stream);
+
+/* ---- whole-image raster / anti-raster sweeps (the reference's
+ *      *PropagationEntireImage kernels, MR.cu:547-753, and iRec1D*,
+ *      IWPP MP DQ/src/MorphologicalReconstruction.cu:817-1074) ------------ */
+/* direction: 0 = +X (left to right), 1 = +Y (top to bottom), 2 = -X, 3 = -Y.
+ * Each applies the propagation rule along the whole row / column (8-conn
+ * also takes the two diagonal pixels of the previous row / column). */
+IWPP_API int iwpp_sweep(void *marker, const void *mask, size_t pitch_marker, size_t pitch_mask, int width,
+                        int height, int dtype, int connectivity, int direction, void *stream);
+/* Times the four sweeps (+X, +Y, -X, -Y) once with CUDA events, like the
+ * reference's one_current_pass (DQ MR.cu:1136-1178); ms_out receives 4
+ * floats. */
+IWPP_API int iwpp_sweep_timing(void *marker, const void *mask, size_t pitch_marker, size_t pitch_mask, int width,
+                               int height, int dtype, int connectivity, float *ms_out);
+
+/* ---- reference-compatible entry points --------------------------------- */
+/* Exactly the reference signature (IWPP MP/include/MorphologicalReconstruction.cuh:45-46;
+ * DQ :53-54, UQ :59-60): uint8, square size x size, 4-connectivity, default
+ * stream, synchronous, in place on marker.  The queue variant is
+ * IWPP_QUEUE_VARIANT (mutex | double | unique), default unique.  Errors are
+ * kept for iwpp_last_status(). */
+IWPP_API void MorphologicalReconstruction(unsigned char *marker, unsigned char *mask, size_t pitchMarker,
+                                          size_t pitchMask, int size);
+/* The reference raises the device heap limit for its in-kernel queue
+ * allocation (IWPP MP/src/globalQueue.cu:3-6).  This library allocates its
+ * queues from the host, so this is a no-op kept for source compatibility. */
+IWPP_API void configureHeapSize(void);
+IWPP_API int iwpp_last_status(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,752 @@
+// iwpp_api.cu -- host side of libiwpp.so: argument checks, workspaces,
+// staging of unaligned images, launch sequencing, CUDA-graph plans and the
+// reference-compatible entry points.  Declarations: include/iwpp.h.
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "iwpp.h"
+#include "iwpp_engine.cuh"
+
+using namespace iwpp;
+
+namespace {
+
+std::atomic<int> g_last_status{IWPP_OK};
+
+int set_last(int s) {
+    g_last_status.store(s);
+    return s;
+}
+
+int bpp_of(int dtype) { return dtype == IWPP_U8 ? 1 : dtype == IWPP_U16 ? 2 : 4; }
+int ppw_of(int dtype) { return dtype == IWPP_U8 ? 4 : dtype == IWPP_U16 ? 2 : 1; }
+
+int default_tile_rows(int dtype) {
+    (void)dtype;
+    return 64;
+}
+
+int resolve_variant(int variant) {
+    if (variant == IWPP_QUEUE_MUTEX || variant == IWPP_QUEUE_DOUBLE || variant == IWPP_QUEUE_UNIQUE) return variant;
+    const char* e = std::getenv("IWPP_QUEUE_VARIANT");
+    if (e) {
+        std::string s(e);
+        if (s == "mutex" || s == "mp" || s == "MP") return IWPP_QUEUE_MUTEX;
+        if (s == "double" || s == "dq" || s == "DQ") return IWPP_QUEUE_DOUBLE;
+        if (s == "unique" || s == "uq" || s == "UQ") return IWPP_QUEUE_UNIQUE;
+    }
+    return IWPP_QUEUE_UNIQUE;
+}
+
+struct Config {
+    int tile_rows;
+    long long queue_capacity;
+    int init_passes;
+    int grid_ctas;
+    int max_restarts;
+    int timeout_ms;
+    int clip_marker;
+};
+
+Config resolve_config(const iwpp_config* c) {
+    Config r;
+    r.tile_rows = c && (c->tile_rows == 32 || c->tile_rows == 64) ? c->tile_rows : 0;
+    r.queue_capacity = c && c->queue_capacity > 0 ? c->queue_capacity : 0;
+    r.init_passes = c && c->init_passes >= 0 ? c->init_passes : 0;
+    r.grid_ctas = c && c->grid_ctas > 0 ? c->grid_ctas : 0;
+    r.max_restarts = c && c->max_restarts > 0 ? c->max_restarts : 64;
+    r.timeout_ms = c && c->timeout_ms > 0 ? c->timeout_ms : 10000;
+    r.clip_marker = c ? c->clip_marker : 0;
+    return r;
+}
+
+bool aligned_for_engine(const void* p, size_t pitch) {
+    return (reinterpret_cast<uintptr_t>(p) & 3u) == 0u && (pitch & 3u) == 0u;
+}
+
+int check_image(const void* marker, const void* mask, size_t pm, size_t pk, int w, int h, int dtype, int conn) {
+    if (dtype != IWPP_U8 && dtype != IWPP_U16 && dtype != IWPP_I32) return IWPP_ERR_INVALID;
+    if (conn != 4 && conn != 8) return IWPP_ERR_INVALID;
+    if (w < 0 || h < 0 || w > (1 << 28) || h > (1 << 28)) return IWPP_ERR_INVALID;
+    if (w == 0 || h == 0) return IWPP_OK;
+    if (!marker || !mask) return IWPP_ERR_INVALID;
+    const size_t row = (size_t)w * (size_t)bpp_of(dtype);
+    if (pm < row || pk < row) return IWPP_ERR_INVALID;
+    if ((reinterpret_cast<uintptr_t>(marker) % (uintptr_t)bpp_of(dtype)) != 0u ||
+        (reinterpret_cast<uintptr_t>(mask) % (uintptr_t)bpp_of(dtype)) != 0u)
+        return IWPP_ERR_INVALID;
+    if (pm % (size_t)bpp_of(dtype) != 0u || pk % (size_t)bpp_of(dtype) != 0u) return IWPP_ERR_INVALID;
+    return IWPP_OK;
+}
+
+int cuda_status(cudaError_t e) {
+    if (e == cudaSuccess) return IWPP_OK;
+    if (e == cudaErrorMemoryAllocation) return IWPP_ERR_OOM;
+    return IWPP_ERR_CUDA;
+}
+
+long long tiles_of(int w, int h, int dtype, int th) {
+    if (w <= 0 || h <= 0) return 0;
+    const long long tw = 32ll * ppw_of(dtype);
+    return ((w + tw - 1) / tw) * (((long long)h + th - 1) / th);
+}
+
+// Device workspace of one job: [Ctrl][ImgDesc x n][state x G][q0][q1].
+struct Workspace {
+    void* base = nullptr;
+    size_t bytes = 0;
+};
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+struct Layout {
+    size_t off_imgs, off_state, off_q0, off_q1, total;
+};
+
+Layout layout_for(long long n_imgs, long long G, long long cap, bool two_queues) {
+    Layout l;
+    l.off_imgs = align_up(sizeof(Ctrl), 256);
+    l.off_state = align_up(l.off_imgs + (size_t)n_imgs * sizeof(ImgDesc), 256);
+    l.off_q0 = align_up(l.off_state + (size_t)G * 4u, 256);
+    l.off_q1 = align_up(l.off_q0 + (size_t)cap * 4u, 256);
+    l.total = align_up(l.off_q1 + (two_queues ? (size_t)cap * 4u : 0u), 256);
+    return l;
+}
+
+long long queue_capacity_for(int variant, long long G, long long requested) {
+    long long cap;
+    if (variant == IWPP_QUEUE_UNIQUE) {
+        cap = std::max<long long>(G, 1);  // one entry per tile at most
+    } else if (requested > 0) {
+        cap = variant == IWPP_QUEUE_MUTEX ? std::max(requested, G) : requested;
+    } else {
+        cap = std::max<long long>(4 * G, 4096);
+    }
+    return std::min<long long>(cap, 0x7fffffffll);
+}
+
+// A job in preparation: descriptors (possibly pointing at staging copies).
+struct Staged {
+    void* user_marker;
+    size_t user_pm;
+    void* buf_m;  // staging copies (nullptr when the user buffer is used)
+    void* buf_k;
+    size_t pitch;
+    int w, h, dtype;
+};
+
+struct Job {
+    std::vector<ImgDesc> descs;
+    std::vector<Staged> staged;
+    long long G = 0;
+    int tile_rows = 64;
+    int variant = IWPP_QUEUE_UNIQUE;
+    Config cfg;
+};
+
+int build_job(Job& job, const iwpp_image* imgs, int n, int variant, const iwpp_config* cfgp, cudaStream_t s,
+              bool allow_staging) {
+    job.cfg = resolve_config(cfgp);
+    job.variant = resolve_variant(variant);
+    int th = job.cfg.tile_rows;
+    if (th == 0) th = n > 0 ? default_tile_rows(imgs[0].dtype) : 64;
+    job.tile_rows = th;
+    long long G = 0;
+    for (int i = 0; i < n; ++i) {
+        const iwpp_image& im = imgs[i];
+        int rc = check_image(im.marker, im.mask, im.pitch_marker, im.pitch_mask, im.width, im.height, im.dtype,
+                             im.connectivity);
+        if (rc != IWPP_OK) return rc;
+    }
+    for (int i = 0; i < n; ++i) {
+        const iwpp_image& im = imgs[i];
+        if (im.width == 0 || im.height == 0) continue;
+        ImgDesc d{};
+        d.marker = static_cast<unsigned char*>(im.marker);
+        d.mask = static_cast<const unsigned char*>(im.mask);
+        d.pitch_m = (long long)im.pitch_marker;
+        d.pitch_k = (long long)im.pitch_mask;
+        d.W = im.width;
+        d.H = im.height;
+        d.dtype = im.dtype;
+        d.conn = im.connectivity;
+        const int tw = 32 * ppw_of(im.dtype);
+        d.tiles_x = (im.width + tw - 1) / tw;
+        d.tiles_y = (im.height + th - 1) / th;
+        d.tile_rows = th;
+        d.tile_base = (int)G;
+        Staged st{im.marker, im.pitch_marker, nullptr, nullptr, 0, im.width, im.height, im.dtype};
+        const bool ok_m = aligned_for_engine(im.marker, im.pitch_marker);
+        const bool ok_k = aligned_for_engine(im.mask, im.pitch_mask);
+        if (!ok_m || !ok_k) {
+            if (!allow_staging) return IWPP_ERR_INVALID;
+            // Rows that do not start on a 4-byte boundary: reconstruct in
+            // aligned copies and copy the marker back afterwards.
+            const size_t row = (size_t)im.width * bpp_of(im.dtype);
+            const size_t pitch = align_up(row, 128);
+            cudaError_t e = cudaMallocAsync(&st.buf_m, pitch * im.height, s);
+            if (e == cudaSuccess) e = cudaMallocAsync(&st.buf_k, pitch * im.height, s);
+            if (e == cudaSuccess)
+                e = cudaMemcpy2DAsync(st.buf_m, pitch, im.marker, im.pitch_marker, row, im.height,
+                                      cudaMemcpyDeviceToDevice, s);
+            if (e == cudaSuccess)
+                e = cudaMemcpy2DAsync(st.buf_k, pitch, im.mask, im.pitch_mask, row, im.height,
+                                      cudaMemcpyDeviceToDevice, s);
+            if (e != cudaSuccess) {
+                if (st.buf_m) cudaFreeAsync(st.buf_m, s);
+                if (st.buf_k) cudaFreeAsync(st.buf_k, s);
+                return cuda_status(e);
+            }
+            st.pitch = pitch;
+            d.marker = static_cast<unsigned char*>(st.buf_m);
+            d.mask = static_cast<const unsigned char*>(st.buf_k);
+            d.pitch_m = (long long)pitch;
+            d.pitch_k = (long long)pitch;
+        }
+        G += (long long)d.tiles_x * d.tiles_y;
+        if (G > 0x7fffffffll) return IWPP_ERR_INVALID;
+        job.descs.push_back(d);
+        job.staged.push_back(st);
+    }
+    job.G = G;
+    return IWPP_OK;
+}
+
+int finish_staging(Job& job, cudaStream_t s) {
+    cudaError_t first = cudaSuccess;
+    for (auto& st : job.staged) {
+        if (!st.buf_m) continue;
+        const size_t row = (size_t)st.w * bpp_of(st.dtype);
+        cudaError_t e = cudaMemcpy2DAsync(st.user_marker, st.user_pm, st.buf_m, st.pitch, row, st.h,
+                                          cudaMemcpyDeviceToDevice, s);
+        if (first == cudaSuccess) first = e;
+        cudaFreeAsync(st.buf_m, s);
+        cudaFreeAsync(st.buf_k, s);
+        st.buf_m = st.buf_k = nullptr;
+    }
+    return cuda_status(first);
+}
+
+}  // namespace
+
+struct iwpp_handle_s {
+    int device = 0;
+    Workspace ws;
+    Ctrl* host_ctrl = nullptr;  // pinned
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaStream_t last_stream = nullptr;
+    long long last_tiles = 0;
+    int last_variant = IWPP_QUEUE_UNIQUE;
+    int last_launch_status = IWPP_OK;
+    bool timed = false;
+    std::mutex mu;
+};
+
+struct iwpp_plan_s {
+    iwpp_handle h = nullptr;
+    Workspace ws;
+    Ctrl* host_ctrl = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t last_stream = nullptr;
+    long long tiles = 0;
+    int variant = IWPP_QUEUE_UNIQUE;
+};
+
+namespace {
+
+int ensure_workspace(Workspace& ws, size_t bytes) {
+    if (ws.bytes >= bytes) return IWPP_OK;
+    if (ws.base) {
+        cudaFree(ws.base);
+        ws.base = nullptr;
+        ws.bytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&ws.base, bytes);
+    if (e != cudaSuccess) {
+        ws.base = nullptr;
+        cudaGetLastError();
+        return cuda_status(e);
+    }
+    ws.bytes = bytes;
+    return IWPP_OK;
+}
+
+int check_device(int device) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return IWPP_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count) return IWPP_ERR_INVALID;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return IWPP_ERR_CUDA;
+    // The kernels are built for sm_103a only.
+    if (!(prop.major == 10 && prop.minor == 3)) return IWPP_ERR_NO_DEVICE;
+    return IWPP_OK;
+}
+
+// Enqueues a prepared job on `s` into workspace `ws`.
+int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool use_events, cudaEvent_t ev0,
+                cudaEvent_t ev1, bool upload_descs) {
+    const bool two = job.variant != IWPP_QUEUE_MUTEX;
+    const long long cap = queue_capacity_for(job.variant, job.G, job.cfg.queue_capacity);
+    const Layout l = layout_for((long long)job.descs.size(), job.G, cap, two);
+    int rc = ensure_workspace(ws, l.total);
+    if (rc != IWPP_OK) return rc;
+    char* base = static_cast<char*>(ws.base);
+    EngineArgs a{};
+    a.imgs = reinterpret_cast<const ImgDesc*>(base + l.off_imgs);
+    a.nimg = (int)job.descs.size();
+    a.G = (unsigned)job.G;
+    a.state = reinterpret_cast<unsigned*>(base + l.off_state);
+    a.q0 = reinterpret_cast<unsigned*>(base + l.off_q0);
+    a.q1 = two ? reinterpret_cast<unsigned*>(base + l.off_q1) : a.q0;
+    a.cap = (unsigned)cap;
+    a.ctrl = reinterpret_cast<Ctrl*>(base);
+    a.timeout_ns = (long long)job.cfg.timeout_ms * 1000000ll;
+    a.max_restarts = job.cfg.max_restarts;
+
+    cudaError_t e = cudaSuccess;
+    if (upload_descs && !job.descs.empty())
+        e = cudaMemcpyAsync(base + l.off_imgs, job.descs.data(), job.descs.size() * sizeof(ImgDesc),
+                            cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_status(e);
+    if (use_events) cudaEventRecord(ev0, s);
+    if (job.cfg.clip_marker)
+        for (const auto& d : job.descs) {
+            e = launch_clip(d, s);
+            if (e != cudaSuccess) return cuda_status(e);
+        }
+    for (int p = 0; p < job.cfg.init_passes; ++p)
+        for (const auto& d : job.descs)
+            for (int dir = 0; dir < 4; ++dir) {
+                // raster (+X, +Y) then anti-raster (-X, -Y)
+                static const int order[4] = {0, 1, 2, 3};
+                e = launch_sweep(d, order[dir], s);
+                if (e != cudaSuccess) return cuda_status(e);
+            }
+    e = engine_launch_init(a, job.variant, s);
+    if (e != cudaSuccess) return cuda_status(e);
+    if (job.G > 0) {
+        LaunchInfo li;
+        e = engine_prepare(job.variant, job.tile_rows, device, &li);
+        if (e != cudaSuccess) return cuda_status(e);
+        long long grid = li.grid;
+        const long long useful = (job.G + kWarps - 1) / kWarps;
+        if (grid > useful) grid = useful;
+        if (job.cfg.grid_ctas > 0 && job.cfg.grid_ctas < grid) grid = job.cfg.grid_ctas;
+        if (grid < 1) grid = 1;
+        e = engine_launch(a, job.variant, job.tile_rows, (int)grid, s);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    if (use_events) cudaEventRecord(ev1, s);
+    return IWPP_OK;
+}
+
+int read_stats(Ctrl* host_ctrl, const Workspace& ws, cudaStream_t s, long long tiles, int variant,
+               iwpp_stats* out, float ms) {
+    cudaError_t e = cudaMemcpyAsync(host_ctrl, ws.base, sizeof(Ctrl), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(e);
+    int st = IWPP_OK;
+    if (host_ctrl->error == DEV_ERR_TIMEOUT) st = IWPP_ERR_TIMEOUT;
+    if (host_ctrl->error == DEV_ERR_OVERFLOW) st = IWPP_ERR_OVERFLOW;
+    if (out) {
+        out->tiles = tiles;
+        out->visits = (long long)host_ctrl->visits;
+        out->sweeps = (long long)host_ctrl->sweeps;
+        out->pushes = (long long)host_ctrl->pushes;
+        out->rounds = (int)host_ctrl->rounds;
+        out->restarts = (int)host_ctrl->restarts;
+        out->status = st;
+        out->variant = variant;
+        out->device_ms = ms;
+    }
+    return st;
+}
+
+iwpp_handle default_handle(int* rc_out) {
+    static std::mutex mu;
+    static iwpp_handle handles[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        *rc_out = IWPP_ERR_NO_DEVICE;
+        return nullptr;
+    }
+    if (dev < 0 || dev >= 64) {
+        *rc_out = IWPP_ERR_INVALID;
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    if (!handles[dev]) {
+        int rc = iwpp_handle_create(&handles[dev], dev);
+        if (rc != IWPP_OK) {
+            *rc_out = rc;
+            return nullptr;
+        }
+    }
+    *rc_out = IWPP_OK;
+    return handles[dev];
+}
+
+int run_job_sync(iwpp_handle h, const iwpp_image* imgs, int n, int variant, const iwpp_config* cfg,
+                 cudaStream_t s, iwpp_stats* stats) {
+    int rc = IWPP_OK;
+    // Arguments are checked before any device is touched; an all-empty job
+    // is complete without one.
+    bool any_pixels = false;
+    for (int i = 0; i < n; ++i) {
+        const iwpp_image& im = imgs[i];
+        rc = check_image(im.marker, im.mask, im.pitch_marker, im.pitch_mask, im.width, im.height, im.dtype,
+                         im.connectivity);
+        if (rc != IWPP_OK) return rc;
+        any_pixels |= im.width > 0 && im.height > 0;
+    }
+    if (!any_pixels) {
+        if (stats) *stats = iwpp_stats{};
+        return IWPP_OK;
+    }
+    if (!h) h = default_handle(&rc);
+    if (!h) return rc;
+    std::lock_guard<std::mutex> lk(h->mu);
+    int prev_dev = 0;
+    cudaGetDevice(&prev_dev);
+    if (prev_dev != h->device) cudaSetDevice(h->device);
+    Job job;
+    rc = build_job(job, imgs, n, variant, cfg, s, true);
+    if (rc == IWPP_OK) rc = enqueue_job(job, h->ws, s, h->device, true, h->ev0, h->ev1, true);
+    const int rc_stage = finish_staging(job, s);
+    if (rc == IWPP_OK) {
+        float ms = 0.f;
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess)
+            rc = cuda_status(e);
+        else {
+            cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+            rc = read_stats(h->host_ctrl, h->ws, s, job.G, job.variant, stats, ms);
+        }
+    } else {
+        cudaStreamSynchronize(s);
+    }
+    if (rc == IWPP_OK) rc = rc_stage;
+    if (prev_dev != h->device) cudaSetDevice(prev_dev);
+    return rc;
+}
+
+}  // namespace
+
+// ====================================================================== API
+extern "C" {
+
+const char* iwpp_status_string(int status) {
+    switch (status) {
+        case IWPP_OK: return "ok";
+        case IWPP_ERR_INVALID: return "invalid argument";
+        case IWPP_ERR_OOM: return "out of device memory";
+        case IWPP_ERR_TIMEOUT: return "a bounded device-side wait timed out";
+        case IWPP_ERR_CUDA: return "CUDA runtime error";
+        case IWPP_ERR_OVERFLOW: return "queue overflow restarts exhausted";
+        case IWPP_ERR_NO_DEVICE: return "no sm_103 (GB300) CUDA device";
+        case IWPP_ERR_BUSY: return "server full or shutting down";
+        default: return "unknown status";
+    }
+}
+
+int iwpp_version(void) { return 1; }
+
+int iwpp_handle_create(iwpp_handle* out, int device) {
+    if (!out) return IWPP_ERR_INVALID;
+    *out = nullptr;
+    int rc = check_device(device);
+    if (rc != IWPP_OK) return rc;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(device);
+    iwpp_handle h = new (std::nothrow) iwpp_handle_s();
+    if (!h) return IWPP_ERR_OOM;
+    h->device = device;
+    cudaError_t e = cudaMallocHost(&h->host_ctrl, sizeof(Ctrl));
+    if (e == cudaSuccess) e = cudaEventCreate(&h->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&h->ev1);
+    cudaSetDevice(prev);
+    if (e != cudaSuccess) {
+        iwpp_handle_destroy(h);
+        return cuda_status(e);
+    }
+    *out = h;
+    return IWPP_OK;
+}
+
+int iwpp_handle_destroy(iwpp_handle h) {
+    if (!h) return IWPP_OK;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(h->device);
+    cudaDeviceSynchronize();
+    if (h->ws.base) cudaFree(h->ws.base);
+    if (h->host_ctrl) cudaFreeHost(h->host_ctrl);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    cudaSetDevice(prev);
+    delete h;
+    return IWPP_OK;
+}
+
+long long iwpp_workspace_bytes(long long tiles, int variant, long long queue_capacity) {
+    const int v = resolve_variant(variant);
+    const long long cap = queue_capacity_for(v, tiles, queue_capacity);
+    return (long long)layout_for(1, tiles, cap, v != IWPP_QUEUE_MUTEX).total;
+}
+
+long long iwpp_tile_count(int width, int height, int dtype, int tile_rows) {
+    if (dtype != IWPP_U8 && dtype != IWPP_U16 && dtype != IWPP_I32) return -1;
+    const int th = tile_rows == 32 || tile_rows == 64 ? tile_rows : default_tile_rows(dtype);
+    return tiles_of(width, height, dtype, th);
+}
+
+int iwpp_reconstruct(iwpp_handle h, void* marker, const void* mask, size_t pitch_marker, size_t pitch_mask,
+                     int width, int height, int dtype, int connectivity, int variant, const iwpp_config* cfg,
+                     void* stream, iwpp_stats* stats) {
+    iwpp_image im{marker, mask, pitch_marker, pitch_mask, width, height, dtype, connectivity};
+    return set_last(run_job_sync(h, &im, 1, variant, cfg, static_cast<cudaStream_t>(stream), stats));
+}
+
+int iwpp_reconstruct_batch(iwpp_handle h, const iwpp_image* images, int n, int variant, const iwpp_config* cfg,
+                           void* stream, iwpp_stats* stats) {
+    if (n < 0 || (n > 0 && !images)) return set_last(IWPP_ERR_INVALID);
+    return set_last(run_job_sync(h, images, n, variant, cfg, static_cast<cudaStream_t>(stream), stats));
+}
+
+int iwpp_reconstruct_async(iwpp_handle h, void* marker, const void* mask, size_t pitch_marker, size_t pitch_mask,
+                           int width, int height, int dtype, int connectivity, int variant, const iwpp_config* cfg,
+                           void* stream) {
+    if (!h) return set_last(IWPP_ERR_INVALID);
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    iwpp_image im{marker, mask, pitch_marker, pitch_mask, width, height, dtype, connectivity};
+    Job job;
+    int rc = build_job(job, &im, 1, variant, cfg, s, true);
+    if (rc == IWPP_OK) rc = enqueue_job(job, h->ws, s, h->device, true, h->ev0, h->ev1, true);
+    const int rc2 = finish_staging(job, s);
+    if (rc == IWPP_OK) rc = rc2;
+    if (rc == IWPP_OK) {
+        // queue the counters copy behind the job; iwpp_handle_sync waits for it
+        cudaError_t e = cudaMemcpyAsync(h->host_ctrl, h->ws.base, sizeof(Ctrl), cudaMemcpyDeviceToHost, s);
+        rc = cuda_status(e);
+    }
+    h->last_stream = s;
+    h->last_tiles = job.G;
+    h->last_variant = job.variant;
+    h->last_launch_status = rc;
+    h->timed = true;
+    return set_last(rc);
+}
+
+int iwpp_handle_sync(iwpp_handle h, iwpp_stats* stats) {
+    if (!h) return set_last(IWPP_ERR_INVALID);
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (h->last_launch_status != IWPP_OK) return set_last(h->last_launch_status);
+    cudaError_t e = cudaStreamSynchronize(h->last_stream);
+    if (e != cudaSuccess) return set_last(cuda_status(e));
+    float ms = 0.f;
+    if (h->timed) cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    const Ctrl& c = *h->host_ctrl;
+    int st = IWPP_OK;
+    if (c.error == DEV_ERR_TIMEOUT) st = IWPP_ERR_TIMEOUT;
+    if (c.error == DEV_ERR_OVERFLOW) st = IWPP_ERR_OVERFLOW;
+    if (stats) {
+        stats->tiles = h->last_tiles;
+        stats->visits = (long long)c.visits;
+        stats->sweeps = (long long)c.sweeps;
+        stats->pushes = (long long)c.pushes;
+        stats->rounds = (int)c.rounds;
+        stats->restarts = (int)c.restarts;
+        stats->status = st;
+        stats->variant = h->last_variant;
+        stats->device_ms = ms;
+    }
+    return set_last(st);
+}
+
+int iwpp_plan_create(iwpp_plan* out, iwpp_handle h, const iwpp_image* images, int n, int variant,
+                     const iwpp_config* cfg) {
+    if (!out || !h || n < 0 || (n > 0 && !images)) return set_last(IWPP_ERR_INVALID);
+    *out = nullptr;
+    std::lock_guard<std::mutex> lk(h->mu);
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(h->device);
+    iwpp_plan p = new (std::nothrow) iwpp_plan_s();
+    if (!p) return set_last(IWPP_ERR_OOM);
+    p->h = h;
+    Job job;
+    cudaStream_t cs = nullptr;
+    int rc = build_job(job, images, n, variant, cfg, nullptr, false);
+    cudaError_t e = cudaSuccess;
+    if (rc == IWPP_OK) {
+        p->tiles = job.G;
+        p->variant = job.variant;
+        e = cudaMallocHost(&p->host_ctrl, sizeof(Ctrl));
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+        rc = cuda_status(e);
+    }
+    if (rc == IWPP_OK) {
+        // Workspace and descriptors first (outside the graph, once).
+        const bool two = job.variant != IWPP_QUEUE_MUTEX;
+        const long long cap = queue_capacity_for(job.variant, job.G, job.cfg.queue_capacity);
+        const Layout l = layout_for((long long)job.descs.size(), job.G, cap, two);
+        rc = ensure_workspace(p->ws, l.total);
+        if (rc == IWPP_OK && !job.descs.empty()) {
+            e = cudaMemcpy(static_cast<char*>(p->ws.base) + l.off_imgs, job.descs.data(),
+                           job.descs.size() * sizeof(ImgDesc), cudaMemcpyHostToDevice);
+            rc = cuda_status(e);
+        }
+        // Warm the kernel attributes before capture.
+        LaunchInfo li;
+        if (rc == IWPP_OK && job.G > 0) rc = cuda_status(engine_prepare(job.variant, job.tile_rows, h->device, &li));
+    }
+    if (rc == IWPP_OK) {
+        e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+        rc = cuda_status(e);
+        if (rc == IWPP_OK) {
+            rc = enqueue_job(job, p->ws, cs, h->device, false, nullptr, nullptr, false);
+            cudaError_t e2 = cudaStreamEndCapture(cs, &p->graph);
+            if (rc == IWPP_OK) rc = cuda_status(e2);
+        }
+        if (rc == IWPP_OK) rc = cuda_status(cudaGraphInstantiate(&p->exec, p->graph, 0));
+    }
+    if (cs) cudaStreamDestroy(cs);
+    cudaSetDevice(prev);
+    if (rc != IWPP_OK) {
+        cudaGetLastError();
+        iwpp_plan_destroy(p);
+        return set_last(rc);
+    }
+    *out = p;
+    return set_last(IWPP_OK);
+}
+
+int iwpp_plan_launch(iwpp_plan p, void* stream) {
+    if (!p || !p->exec) return set_last(IWPP_ERR_INVALID);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaGraphLaunch(p->exec, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p->host_ctrl, p->ws.base, sizeof(Ctrl), cudaMemcpyDeviceToHost, s);
+    p->last_stream = s;
+    return set_last(cuda_status(e));
+}
+
+int iwpp_plan_sync(iwpp_plan p, iwpp_stats* stats) {
+    if (!p) return set_last(IWPP_ERR_INVALID);
+    cudaError_t e = cudaStreamSynchronize(p->last_stream);
+    if (e != cudaSuccess) return set_last(cuda_status(e));
+    const Ctrl& c = *p->host_ctrl;
+    int st = IWPP_OK;
+    if (c.error == DEV_ERR_TIMEOUT) st = IWPP_ERR_TIMEOUT;
+    if (c.error == DEV_ERR_OVERFLOW) st = IWPP_ERR_OVERFLOW;
+    if (stats) {
+        stats->tiles = p->tiles;
+        stats->visits = (long long)c.visits;
+        stats->sweeps = (long long)c.sweeps;
+        stats->pushes = (long long)c.pushes;
+        stats->rounds = (int)c.rounds;
+        stats->restarts = (int)c.restarts;
+        stats->status = st;
+        stats->variant = p->variant;
+        stats->device_ms = 0.0;
+    }
+    return set_last(st);
+}
+
+int iwpp_plan_destroy(iwpp_plan p) {
+    if (!p) return IWPP_OK;
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->ws.base) cudaFree(p->ws.base);
+    if (p->host_ctrl) cudaFreeHost(p->host_ctrl);
+    delete p;
+    return IWPP_OK;
+}
+
+int iwpp_clip(void* marker, const void* mask, size_t pitch_marker, size_t pitch_mask, int width, int height,
+              int dtype, void* stream) {
+    int rc = check_image(marker, mask, pitch_marker, pitch_mask, width, height, dtype, 4);
+    if (rc != IWPP_OK) return set_last(rc);
+    ImgDesc d{};
+    d.marker = static_cast<unsigned char*>(marker);
+    d.mask = static_cast<const unsigned char*>(mask);
+    d.pitch_m = (long long)pitch_marker;
+    d.pitch_k = (long long)pitch_mask;
+    d.W = width;
+    d.H = height;
+    d.dtype = dtype;
+    d.conn = 4;
+    if (!aligned_for_engine(marker, pitch_marker) || !aligned_for_engine(mask, pitch_mask)) {
+        // byte-granular rows: one thread per pixel via a pixel-sized view
+        // is not needed for correctness here; route through staging
+        iwpp_image im{marker, mask, pitch_marker, pitch_mask, width, height, dtype, 4};
+        Job job;
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        iwpp_config c{};
+        rc = build_job(job, &im, 1, IWPP_QUEUE_UNIQUE, &c, s, true);
+        if (rc == IWPP_OK && !job.descs.empty()) rc = cuda_status(launch_clip(job.descs[0], s));
+        const int rc2 = finish_staging(job, s);
+        return set_last(rc == IWPP_OK ? rc2 : rc);
+    }
+    return set_last(cuda_status(launch_clip(d, static_cast<cudaStream_t>(stream))));
+}
+
+int iwpp_sweep(void* marker, const void* mask, size_t pitch_marker, size_t pitch_mask, int width, int height,
+               int dtype, int connectivity, int direction, void* stream) {
+    int rc = check_image(marker, mask, pitch_marker, pitch_mask, width, height, dtype, connectivity);
+    if (rc != IWPP_OK) return set_last(rc);
+    if (direction < 0 || direction > 3) return set_last(IWPP_ERR_INVALID);
+    iwpp_image im{marker, mask, pitch_marker, pitch_mask, width, height, dtype, connectivity};
+    Job job;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    iwpp_config c{};
+    rc = build_job(job, &im, 1, IWPP_QUEUE_UNIQUE, &c, s, true);
+    if (rc == IWPP_OK && !job.descs.empty()) rc = cuda_status(launch_sweep(job.descs[0], direction, s));
+    const int rc2 = finish_staging(job, s);
+    return set_last(rc == IWPP_OK ? rc2 : rc);
+}
+
+int iwpp_sweep_timing(void* marker, const void* mask, size_t pitch_marker, size_t pitch_mask, int width,
+                      int height, int dtype, int connectivity, float* ms_out) {
+    if (!ms_out) return set_last(IWPP_ERR_INVALID);
+    cudaEvent_t ev[5];
+    for (auto& e : ev) cudaEventCreate(&e);
+    int rc = IWPP_OK;
+    cudaEventRecord(ev[0], nullptr);
+    for (int dir = 0; dir < 4 && rc == IWPP_OK; ++dir) {
+        rc = iwpp_sweep(marker, mask, pitch_marker, pitch_mask, width, height, dtype, connectivity, dir, nullptr);
+        cudaEventRecord(ev[dir + 1], nullptr);
+    }
+    if (rc == IWPP_OK) {
+        cudaError_t e = cudaEventSynchronize(ev[4]);
+        rc = cuda_status(e);
+        for (int dir = 0; dir < 4 && rc == IWPP_OK; ++dir) cudaEventElapsedTime(&ms_out[dir], ev[dir], ev[dir + 1]);
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    return set_last(rc);
+}
+
+void MorphologicalReconstruction(unsigned char* marker, unsigned char* mask, size_t pitchMarker, size_t pitchMask,
+                                 int size) {
+    iwpp_image im{marker, mask, pitchMarker, pitchMask, size, size, IWPP_U8, 4};
+    set_last(run_job_sync(nullptr, &im, 1, IWPP_QUEUE_DEFAULT, nullptr, nullptr, nullptr));
+}
+
+void configureHeapSize(void) {}
+
+int iwpp_last_status(void) { return g_last_status.load(); }
+
+}  // extern "C"

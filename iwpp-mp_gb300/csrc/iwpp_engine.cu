@@ -1,0 +1,471 @@
+// iwpp_engine.cu -- device side of the persistent tile engine (see
+// iwpp_engine.cuh for the design and the reference citations).
+#include <cstdio>
+
+#include "iwpp_engine.cuh"
+
+namespace iwpp {
+
+__device__ __forceinline__ long long globaltimer_ns() {
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned ld_volatile(const unsigned* p) { return *(const volatile unsigned*)p; }
+__device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
+
+__device__ __forceinline__ void set_error(Ctrl* c, unsigned code) { atomicCAS(&c->error, 0u, code); }
+
+// Image of global tile g: the last image whose tile_base <= g.
+__device__ __forceinline__ int find_image(const EngineArgs& a, unsigned g) {
+    int lo = 0, hi = a.nimg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((unsigned)__ldg(&a.imgs[mid].tile_base) <= g)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int TH>
+__device__ __forceinline__ VisitResult dispatch_visit(const ImgDesc& d, int tx, int ty, WarpSmem<TH>& sm, int lane) {
+    const int mode = d.dtype * 2 + (d.conn == 8 ? 1 : 0);
+    switch (mode) {
+        case 0: return visit_tile<DT_U8, 4, TH>(d, tx, ty, sm, lane);
+        case 1: return visit_tile<DT_U8, 8, TH>(d, tx, ty, sm, lane);
+        case 2: return visit_tile<DT_U16, 4, TH>(d, tx, ty, sm, lane);
+        case 3: return visit_tile<DT_U16, 8, TH>(d, tx, ty, sm, lane);
+        case 4: return visit_tile<DT_I32, 4, TH>(d, tx, ty, sm, lane);
+        default: return visit_tile<DT_I32, 8, TH>(d, tx, ty, sm, lane);
+    }
+}
+
+struct WarpCounters {
+    unsigned long long visits = 0, sweeps = 0, pushes = 0;
+};
+
+// ---------------------------------------------------------------- mutex
+// Bounded spin on the global mutex (IWPP MP/src/globalQueue.cu:35, :114 spin
+// without a bound; here a wall-clock bound ends in DEV_ERR_TIMEOUT).
+__device__ bool mutex_lock(const EngineArgs& a) {
+    const long long t0 = globaltimer_ns();
+    unsigned ns = 32;
+    while (atomicCAS(&a.ctrl->lock, 0, 1) != 0) {
+        __nanosleep(ns);
+        if (ns < 1024) ns <<= 1;
+        if (ld_volatile(&a.ctrl->error) != 0u) return false;
+        if (globaltimer_ns() - t0 > a.timeout_ns) {
+            set_error(a.ctrl, DEV_ERR_TIMEOUT);
+            return false;
+        }
+    }
+    __threadfence();
+    return true;
+}
+
+__device__ __forceinline__ void mutex_unlock(const EngineArgs& a) {
+    __threadfence();
+    atomicExch(&a.ctrl->lock, 0);
+}
+
+// ---------------------------------------------------------------- notify
+// Marks the neighbour tiles in `nb` DIRTY and inserts them into the queue
+// (VAR_UNIQUE: only tiles that were neither pending nor being visited).
+// One lane per direction, one queue reservation per warp.
+template <int VAR>
+__device__ void notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty, unsigned nb, int lane, unsigned* wq,
+                       WarpCounters& cnt) {
+    bool want = false;
+    unsigned gn = 0u;
+    if (lane < 8 && ((nb >> lane) & 1u)) {
+        const int nx = tx + kNbDx[lane], ny = ty + kNbDy[lane];
+        if (nx >= 0 && nx < d.tiles_x && ny >= 0 && ny < d.tiles_y) {
+            gn = (unsigned)d.tile_base + (unsigned)(ny * d.tiles_x + nx);
+            const unsigned old = atomicOr(&a.state[gn], ST_DIRTY);
+            want = VAR == VAR_UNIQUE ? (old & (ST_DIRTY | ST_ACTIVE)) == 0u : true;
+        }
+    }
+    const unsigned ballot = __ballot_sync(FULL, want);
+    if (ballot == 0u) return;
+    const int n = __popc(ballot);
+    const int rank = __popc(ballot & ((1u << lane) - 1u));
+    if (VAR == VAR_MUTEX) {
+        // IWPP MP/src/globalQueue.cu:25-81: all n entries under one lock
+        int base = -1;
+        if (lane == 0) {
+            if (mutex_lock(a)) {
+                const int top = ld_volatile(&a.ctrl->top);
+                if ((unsigned)top + (unsigned)n <= a.cap) {
+                    base = top;
+                    atomicAdd(&a.ctrl->pending, n);  // before the entries can be taken
+                } else {
+                    atomicExch(&a.ctrl->overflow, 1u);  // MR.cu:524-526 (memLeak)
+                    mutex_unlock(a);
+                }
+            }
+        }
+        base = __shfl_sync(FULL, base, 0);
+        if (base < 0) return;
+        if (want) a.q0[base + rank] = gn;
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence();
+            *(volatile int*)&a.ctrl->top = base + n;
+            mutex_unlock(a);
+        }
+        cnt.pushes += (unsigned)n;
+    } else {
+        // IWPP MP DQ/src/globalQueue.cu:14-47, aggregated per warp
+        unsigned base = 0u;
+        if (lane == 0) base = atomicAdd(&a.ctrl->wn, (unsigned)n);
+        base = __shfl_sync(FULL, base, 0);
+        if (want) {
+            const unsigned pos = base + (unsigned)rank;
+            if (pos < a.cap)
+                wq[pos] = gn;
+            else
+                atomicExch(&a.ctrl->overflow, 1u);
+        }
+        cnt.pushes += (unsigned)n;
+    }
+}
+
+// ------------------------------------------------------------ one entry
+// Takes tile g (if no other warp owns it) and visits it until it is clean.
+template <int VAR, int TH>
+__device__ void process_entry(const EngineArgs& a, unsigned g, WarpSmem<TH>& sm, int lane, unsigned* wq,
+                              WarpCounters& cnt) {
+    unsigned old = 0u;
+    if (lane == 0) old = atomicOr(&a.state[g], ST_ACTIVE);
+    old = __shfl_sync(FULL, old, 0);
+    if (old & ST_ACTIVE) return;  // owned elsewhere; DIRTY is set and the owner revisits
+
+    const int ii = find_image(a, g);
+    const ImgDesc d = a.imgs[ii];
+    const int t = (int)(g - (unsigned)d.tile_base);
+    const int ty = t / d.tiles_x, tx = t - ty * d.tiles_x;
+    for (;;) {
+        if (lane == 0) old = atomicAnd(&a.state[g], ~ST_DIRTY);
+        old = __shfl_sync(FULL, old, 0);
+        if ((old & ST_DIRTY) == 0u) {
+            unsigned prev = 0u;
+            if (lane == 0) prev = atomicCAS(&a.state[g], ST_ACTIVE, 0u);
+            prev = __shfl_sync(FULL, prev, 0);
+            if (prev == ST_ACTIVE) return;
+            continue;  // DIRTY came back: visit again
+        }
+        __threadfence();
+        __syncwarp();
+        const VisitResult r = dispatch_visit<TH>(d, tx, ty, sm, lane);
+        cnt.visits += 1;
+        cnt.sweeps += r.sweeps;
+        if (r.nb != 0u) {
+            __threadfence();  // this tile's stores before the neighbours' DIRTY
+            __syncwarp();
+            notify<VAR>(a, d, tx, ty, r.nb, lane, wq, cnt);
+        }
+    }
+}
+
+// ------------------------------------------------------- mutex worker
+// One persistent launch; warps take up to kMutexBatch entries per lock
+// acquisition from the LIFO stack (the reference takes one,
+// IWPP MP/src/MorphologicalReconstruction.cu:221).  Termination: the stack
+// is empty and no taken entry is unfinished (`pending` == 0), which replaces
+// activeBlocksCount (IWPP MP/src/globalQueue.cu:134-145).  On overflow the
+// quiescent stack is refilled with every tile (MR.cu:785-806).
+template <int TH>
+__device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, WarpCounters& cnt) {
+    long long idle_since = 0;
+    unsigned idle_progress = 0u;
+    unsigned ns = 64;
+    for (;;) {
+        int n = 0, base = 0, verdict = 0;  // verdict: 0 work/retry, 1 exit, 2 refill
+        if (lane == 0) {
+            if (!mutex_lock(a)) {
+                verdict = 1;
+            } else {
+                const int top = ld_volatile(&a.ctrl->top);
+                if (top > 0) {
+                    n = top < kMutexBatch ? top : kMutexBatch;
+                    base = top - n;
+                } else if (ld_volatile(&a.ctrl->pending) == 0) {
+                    if (ld_volatile(&a.ctrl->overflow) != 0u) {
+                        if ((int)ld_volatile(&a.ctrl->restarts) >= a.max_restarts) {
+                            set_error(a.ctrl, DEV_ERR_OVERFLOW);
+                            verdict = 1;
+                        } else {
+                            verdict = 2;
+                        }
+                    } else {
+                        verdict = 1;
+                    }
+                }
+                if (n == 0 && verdict != 2) mutex_unlock(a);
+            }
+        }
+        n = __shfl_sync(FULL, n, 0);
+        base = __shfl_sync(FULL, base, 0);
+        verdict = __shfl_sync(FULL, verdict, 0);
+        if (verdict == 1) return;
+        if (verdict == 2) {
+            // quiescent with lost insertions: refill with every tile (lock held)
+            for (unsigned i = (unsigned)lane; i < a.G && i < a.cap; i += 32u) a.q0[i] = a.G - 1u - i;
+            __syncwarp();
+            if (lane == 0) {
+                const int cnt_all = (int)(a.G < a.cap ? a.G : a.cap);
+                atomicAdd(&a.ctrl->pending, cnt_all);
+                atomicExch(&a.ctrl->overflow, 0u);
+                atomicAdd(&a.ctrl->restarts, 1u);
+                __threadfence();
+                *(volatile int*)&a.ctrl->top = cnt_all;
+                mutex_unlock(a);
+            }
+            __syncwarp();
+            continue;
+        }
+        if (n == 0) {
+            // nothing to take but work in flight: back off, bounded by progress
+            const unsigned prog = ld_volatile(&a.ctrl->progress);
+            const long long now = globaltimer_ns();
+            if (idle_since == 0 || prog != idle_progress) {
+                idle_since = now;
+                idle_progress = prog;
+            } else if (now - idle_since > a.timeout_ns) {
+                if (lane == 0) set_error(a.ctrl, DEV_ERR_TIMEOUT);
+                return;
+            }
+            if (ld_volatile(&a.ctrl->error) != 0u) return;
+            __nanosleep(ns);
+            if (ns < 2048) ns <<= 1;
+            continue;
+        }
+        idle_since = 0;
+        ns = 64;
+        // copy the taken entries out before the lock is released
+        unsigned mine = 0u;
+        if (lane < n) mine = a.q0[base + lane];
+        __syncwarp();
+        if (lane == 0) {
+            *(volatile int*)&a.ctrl->top = base;
+            mutex_unlock(a);
+        }
+        for (int j = 0; j < n; ++j) {
+            const unsigned g = __shfl_sync(FULL, mine, j);
+            process_entry<VAR_MUTEX, TH>(a, g, sm, lane, nullptr, cnt);
+            if (lane == 0) {
+                __threadfence();
+                atomicAdd(&a.ctrl->progress, 1u);
+                atomicSub(&a.ctrl->pending, 1);  // after this entry's insertions
+            }
+        }
+    }
+}
+
+// --------------------------------------------------------- grid barrier
+// All CTAs of the (cooperative) launch.  The last CTA to arrive performs the
+// round transition.  Waits are bounded; returns false when the job failed.
+__device__ bool grid_barrier_round(const EngineArgs& a) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Ctrl* c = a.ctrl;
+        int ok = 1;
+        const unsigned gen = ld_volatile(&c->bar_gen);
+        __threadfence();
+        const unsigned arrived = atomicAdd(&c->bar_count, 1u);
+        if (arrived == gridDim.x - 1u) {
+            // Round transition (IWPP MP DQ/src/globalQueue.cu:139-157 swapQueues,
+            // UQ/src/globalQueue.cu:159-168 resetReadQueue, and the overflow
+            // restart of DQ/MR.cu:1242-1323, all on the device).
+            __threadfence();
+            const unsigned wn = ld_volatile(&c->wn);
+            unsigned rn;
+            if (ld_volatile(&c->overflow) != 0u) {
+                if ((int)c->restarts >= a.max_restarts) {
+                    set_error(c, DEV_ERR_OVERFLOW);
+                    rn = 0u;
+                } else {
+                    c->restarts += 1u;
+                    c->vfull = 1u;
+                    rn = a.G;
+                }
+                c->overflow = 0u;
+            } else {
+                c->vfull = 0u;
+                rn = wn < a.cap ? wn : a.cap;
+            }
+            c->qsel ^= 1u;
+            c->rn = rn;
+            c->wn = 0u;
+            c->rcur = 0u;
+            c->rounds += 1u;
+            if (rn == 0u || ld_volatile(&c->error) != 0u) c->done = 1u;
+            c->bar_count = 0u;
+            __threadfence();
+            atomicAdd(&c->bar_gen, 1u);
+        } else {
+            const long long t0 = globaltimer_ns();
+            unsigned ns = 64;
+            while (ld_volatile(&c->bar_gen) == gen) {
+                __nanosleep(ns);
+                if (ns < 2048) ns <<= 1;
+                if (ld_volatile(&c->error) != 0u) {
+                    ok = 0;
+                    break;
+                }
+                if (globaltimer_ns() - t0 > a.timeout_ns) {
+                    set_error(c, DEV_ERR_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
+            }
+            __threadfence();
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// ------------------------------------------------------- round worker
+template <int VAR, int TH>
+__device__ void round_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, WarpCounters& cnt) {
+    for (;;) {
+        const unsigned rn = ld_volatile(&a.ctrl->rn);
+        const unsigned vfull = ld_volatile(&a.ctrl->vfull);
+        const unsigned qsel = ld_volatile(&a.ctrl->qsel);
+        const unsigned* rq = qsel ? a.q1 : a.q0;
+        unsigned* wq = qsel ? a.q0 : a.q1;
+        for (;;) {
+            unsigned idx = 0u;
+            if (lane == 0) idx = atomicAdd(&a.ctrl->rcur, 1u);
+            idx = __shfl_sync(FULL, idx, 0);
+            if (idx >= rn) break;
+            if (ld_volatile(&a.ctrl->error) != 0u) break;
+            const unsigned g = vfull ? idx : __ldcg(&rq[idx]);
+            process_entry<VAR, TH>(a, g, sm, lane, wq, cnt);
+        }
+        if (!grid_barrier_round(a)) return;
+        if (ld_volatile(&a.ctrl->done) != 0u) return;
+    }
+}
+
+// --------------------------------------------------------------- kernels
+template <int VAR, int TH>
+__global__ void __launch_bounds__(kWarps * 32) engine_kernel(EngineArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    WarpSmem<TH>& sm = reinterpret_cast<WarpSmem<TH>*>(smem_raw)[warp];
+    WarpCounters cnt;
+    if (VAR == VAR_MUTEX)
+        mutex_worker<TH>(a, sm, lane, cnt);
+    else
+        round_worker<VAR, TH>(a, sm, lane, cnt);
+    if (lane == 0) {
+        if (cnt.visits) atomicAdd(&a.ctrl->visits, cnt.visits);
+        if (cnt.sweeps) atomicAdd(&a.ctrl->sweeps, cnt.sweeps);
+        if (cnt.pushes) atomicAdd(&a.ctrl->pushes, cnt.pushes);
+    }
+}
+
+// Job initialisation: every tile DIRTY; round 0 (double / unique) is the
+// virtual list of all tiles; the mutex stack holds every tile so that the
+// first pops come out in raster order (IWPP MP/src/globalQueue.cu:83-97,
+// initFillGlobalQueue).
+__global__ void engine_init_kernel(EngineArgs a, int variant) {
+    const unsigned stride = gridDim.x * blockDim.x;
+    for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < a.G; g += stride) {
+        a.state[g] = ST_DIRTY;
+        if (variant == VAR_MUTEX && g < a.cap) a.q0[g] = a.G - 1u - g;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        Ctrl* c = a.ctrl;
+        c->rn = a.G;
+        c->wn = 0u;
+        c->rcur = 0u;
+        c->qsel = 0u;
+        c->vfull = 1u;
+        c->done = a.G == 0u ? 1u : 0u;
+        c->overflow = a.G > a.cap && variant == VAR_MUTEX ? 1u : 0u;
+        c->restarts = 0u;
+        c->rounds = 0u;
+        c->bar_count = 0u;
+        c->bar_gen = 0u;
+        c->error = 0u;
+        c->lock = 0;
+        c->top = (int)(a.G < a.cap ? a.G : a.cap);
+        c->pending = (int)(a.G < a.cap ? a.G : a.cap);
+        c->progress = 0u;
+        c->visits = 0ull;
+        c->sweeps = 0ull;
+        c->pushes = 0ull;
+    }
+}
+
+// ------------------------------------------------------------ host side
+template <int VAR, int TH>
+static void* kernel_ptr() {
+    return reinterpret_cast<void*>(&engine_kernel<VAR, TH>);
+}
+
+static void* select_kernel(int variant, int tile_rows) {
+    if (tile_rows == 32) {
+        if (variant == VAR_MUTEX) return kernel_ptr<VAR_MUTEX, 32>();
+        if (variant == VAR_DOUBLE) return kernel_ptr<VAR_DOUBLE, 32>();
+        return kernel_ptr<VAR_UNIQUE, 32>();
+    }
+    if (variant == VAR_MUTEX) return kernel_ptr<VAR_MUTEX, 64>();
+    if (variant == VAR_DOUBLE) return kernel_ptr<VAR_DOUBLE, 64>();
+    return kernel_ptr<VAR_UNIQUE, 64>();
+}
+
+static size_t smem_bytes(int tile_rows) {
+    return tile_rows == 32 ? kWarps * sizeof(WarpSmem<32>) : kWarps * sizeof(WarpSmem<64>);
+}
+
+cudaError_t engine_prepare(int variant, int tile_rows, int device, LaunchInfo* li) {
+    void* k = select_kernel(variant, tile_rows);
+    const size_t smem = smem_bytes(tile_rows);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kWarps * 32, smem);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) return e;
+    li->grid = per_sm * sms;
+    li->block = kWarps * 32;
+    li->smem = smem;
+    return li->grid > 0 ? cudaSuccess : cudaErrorInvalidConfiguration;
+}
+
+cudaError_t engine_launch_init(const EngineArgs& a, int variant, cudaStream_t s) {
+    unsigned blocks = (a.G + 255u) / 256u;
+    if (blocks == 0u) blocks = 1u;
+    if (blocks > 4096u) blocks = 4096u;
+    engine_init_kernel<<<blocks, 256, 0, s>>>(a, variant);
+    return cudaGetLastError();
+}
+
+cudaError_t engine_launch(const EngineArgs& a, int variant, int tile_rows, int grid, cudaStream_t s) {
+    void* k = select_kernel(variant, tile_rows);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kWarps * 32);
+    cfg.dynamicSmemBytes = smem_bytes(tile_rows);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    EngineArgs args = a;
+    void* params[] = {&args};
+    return cudaLaunchKernelExC(&cfg, k, params);
+}
+
+}  // namespace iwpp

@@ -1,0 +1,89 @@
+// iwpp_engine.cuh -- the persistent tile engine and its three work queues.
+//
+// Reference counterparts:
+//   MUTEX  IWPP MP/src/globalQueue.cu:25-81 (insert under a spin mutex),
+//          :100-155 (read one entry under the mutex, activeBlocksCount
+//          termination), MR.cu:163-542 (one persistent launch), overflow
+//          restart MR.cu:785-806.
+//   DOUBLE IWPP MP DQ/src/globalQueue.cu:14-47 (atomicAdd reservation),
+//          :139-157 (swapQueues), MR.cu:1242-1323 (one launch per round,
+//          host reads the queue size back every round).
+//   UNIQUE IWPP MP UQ/src/MorphologicalReconstruction.cu:1152-1293
+//          (per-tile flag de-duplication between rounds).
+//
+// GB300 form: one persistent launch for all three.  The double / unique
+// rounds are separated by a device-wide barrier (cooperative launch) instead
+// of a host round trip, the unique queue de-duplicates when a tile is
+// inserted, and all insertions are warp-aggregated (one atomic per warp).
+//
+// Tile ownership.  Each tile has a state word: DIRTY (needs a visit) and
+// ACTIVE (a warp is visiting it).  A warp that takes a tile sets ACTIVE; if
+// it was already set the entry is dropped (the owner will see DIRTY and
+// revisit).  The owner clears DIRTY before it reads the tile and releases
+// with CAS(ACTIVE -> 0), revisiting while DIRTY reappears.  So at most one
+// warp writes a tile's pixels, with plain stores, and every write that can
+// raise a neighbour is followed by DIRTY on that neighbour after a fence.
+#pragma once
+
+#include "iwpp_device.cuh"
+
+namespace iwpp {
+
+enum : unsigned { ST_DIRTY = 1u, ST_ACTIVE = 2u };
+enum : int { VAR_MUTEX = 0, VAR_DOUBLE = 1, VAR_UNIQUE = 2 };
+enum : unsigned { DEV_OK = 0u, DEV_ERR_TIMEOUT = 3u, DEV_ERR_OVERFLOW = 5u };
+
+constexpr int kWarps = 4;       // warps (independent tile workers) per CTA
+constexpr int kMutexBatch = 8;  // entries taken per mutex acquisition
+
+struct Ctrl {
+    unsigned rn;        // entries in the read queue (this round)
+    unsigned wn;        // insertions into the write queue (may exceed cap)
+    unsigned rcur;      // read cursor
+    unsigned qsel;      // read queue = qsel ? q1 : q0
+    unsigned vfull;     // the read queue is every tile 0..G-1
+    unsigned done;
+    unsigned overflow;  // an insertion did not fit since the last restart
+    unsigned restarts;
+    unsigned rounds;
+    unsigned bar_count;
+    unsigned bar_gen;
+    unsigned error;
+    int lock;           // mutex stack
+    int top;
+    int pending;        // mutex: entries in the stack or taken and unfinished
+    unsigned progress;  // finished entries (for the no-progress timeout)
+    unsigned long long visits;
+    unsigned long long sweeps;
+    unsigned long long pushes;
+    unsigned long long pad;
+};
+
+struct EngineArgs {
+    const ImgDesc* imgs;
+    int nimg;
+    unsigned G;         // tiles in the job
+    unsigned* state;    // G tile state words
+    unsigned* q0;       // queue buffers, cap entries each
+    unsigned* q1;
+    unsigned cap;
+    Ctrl* ctrl;
+    long long timeout_ns;
+    int max_restarts;
+};
+
+}  // namespace iwpp
+
+// Host-side entry points implemented in iwpp_engine.cu.
+namespace iwpp {
+struct LaunchInfo {
+    int grid;
+    int block;
+    size_t smem;
+};
+cudaError_t engine_prepare(int variant, int tile_rows, int device, LaunchInfo* li);
+cudaError_t engine_launch_init(const EngineArgs& a, int variant, cudaStream_t s);
+cudaError_t engine_launch(const EngineArgs& a, int variant, int tile_rows, int grid, cudaStream_t s);
+cudaError_t launch_clip(const ImgDesc& d, cudaStream_t s);
+cudaError_t launch_sweep(const ImgDesc& d, int direction, cudaStream_t s);
+}  // namespace iwpp

@@ -1,0 +1,185 @@
+// iwpp_sweeps.cu -- elementwise precondition clip and whole-image directional
+// sweeps.
+//
+// clip:   the reference's clipImage (IWPP MP/src/MorphologicalReconstruction.cu:827-836),
+//         marker = min(marker, mask), one 32-bit word per thread.
+// sweeps: the reference's *PropagationEntireImage kernels (MR.cu:547-753)
+//         and the iRec1D* alternatives (IWPP MP DQ/src/MorphologicalReconstruction.cu:817-1074),
+//         rule m = max(m, min(prev, mask)) along one axis.
+//   +X / -X: one warp per row, the whole row as one max-min scan (128-byte
+//            chunks, carry from chunk to chunk), exact and coalesced.
+//   +Y / -Y: one warp per 128-byte column strip walking the full height;
+//            8-connectivity also takes the two diagonal pixels of the
+//            previous row inside the strip.  Every pixel is written by one
+//            thread, so the result is deterministic.
+#include "iwpp_engine.cuh"
+
+namespace iwpp {
+
+template <int DT>
+__device__ __forceinline__ void load_word_plain(const unsigned char* mrow, const unsigned char* krow, int npx,
+                                                uint32_t& mw, uint32_t& kw) {
+    using P = Px<DT>;
+    if (npx >= P::PPW) {
+        mw = *reinterpret_cast<const unsigned int*>(mrow);
+        kw = __ldg(reinterpret_cast<const unsigned int*>(krow));
+    } else {
+        mw = P::PPW == 1 ? P::MINW : 0u;
+        kw = P::PPW == 1 ? P::MINW : 0u;
+#pragma unroll
+        for (int i = 0; i < P::PPW; ++i) {
+            if (i < npx) {
+                mw |= P::ld_px(mrow + i * P::BPP) << (8 * P::BPP * i);
+                kw |= P::ld_px(krow + i * P::BPP) << (8 * P::BPP * i);
+            }
+        }
+    }
+}
+
+template <int DT>
+__device__ __forceinline__ void store_word_plain(unsigned char* mrow, int npx, uint32_t w) {
+    using P = Px<DT>;
+    if (npx >= P::PPW) {
+        *reinterpret_cast<unsigned int*>(mrow) = w;
+    } else {
+#pragma unroll
+        for (int i = 0; i < P::PPW; ++i)
+            if (i < npx) P::st_px(mrow + i * P::BPP, P::get(w, i));
+    }
+}
+
+// ------------------------------------------------------------------- clip
+template <int DT>
+__global__ void clip_kernel(ImgDesc d) {
+    using P = Px<DT>;
+    const int words = (d.W + P::PPW - 1) / P::PPW;
+    const long long total = (long long)words * d.H;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int y = (int)(i / words), wi = (int)(i - (long long)y * words);
+        const int px0 = wi * P::PPW, npx = d.W - px0;
+        unsigned char* mrow = d.marker + (size_t)y * d.pitch_m + (size_t)px0 * P::BPP;
+        const unsigned char* krow = d.mask + (size_t)y * d.pitch_k + (size_t)px0 * P::BPP;
+        uint32_t mw, kw;
+        load_word_plain<DT>(mrow, krow, npx, mw, kw);
+        const uint32_t c = P::vmin(mw, kw);
+        if (c != mw) store_word_plain<DT>(mrow, npx, c);
+    }
+}
+
+// --------------------------------------------------------------- X sweeps
+template <int DT, bool FWD>
+__global__ void sweep_x_kernel(ImgDesc d) {
+    using P = Px<DT>;
+    constexpr int TW = 32 * P::PPW;
+    const int lane = threadIdx.x & 31;
+    const int row = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (row >= d.H) return;
+    const int chunks = (d.W + TW - 1) / TW;
+    unsigned char* mbase = d.marker + (size_t)row * d.pitch_m;
+    const unsigned char* kbase = d.mask + (size_t)row * d.pitch_k;
+    uint32_t carry = P::MINPX;
+    for (int cc = 0; cc < chunks; ++cc) {
+        const int c = FWD ? cc : chunks - 1 - cc;
+        const int px0 = c * TW + lane * P::PPW, npx = d.W - px0;
+        uint32_t mw = P::MINW, kw = P::MINW;
+        if (npx > 0) load_word_plain<DT>(mbase + (size_t)px0 * P::BPP, kbase + (size_t)px0 * P::BPP, npx, mw, kw);
+        const uint32_t nw = hscan<DT, FWD>(mw, kw, carry, lane);
+        if (npx > 0 && nw != mw) store_word_plain<DT>(mbase + (size_t)px0 * P::BPP, npx, nw);
+        carry = FWD ? __shfl_sync(FULL, P::last(nw), 31) : __shfl_sync(FULL, P::first(nw), 0);
+    }
+}
+
+// --------------------------------------------------------------- Y sweeps
+template <int DT, int CONN, bool DOWN>
+__global__ void sweep_y_kernel(ImgDesc d) {
+    using P = Px<DT>;
+    constexpr int TW = 32 * P::PPW;
+    const int lane = threadIdx.x & 31;
+    const int strip = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int strips = (d.W + TW - 1) / TW;
+    if (strip >= strips) return;
+    const int px0 = strip * TW + lane * P::PPW, npx = d.W - px0;
+    const size_t off = (size_t)(npx > 0 ? px0 : 0) * P::BPP;
+    uint32_t prev = P::MINW;
+    for (int i = 0; i < d.H; ++i) {
+        const int y = DOWN ? i : d.H - 1 - i;
+        uint32_t mw = P::MINW, kw = P::MINW;
+        unsigned char* mrow = d.marker + (size_t)y * d.pitch_m + off;
+        if (npx > 0) load_word_plain<DT>(mrow, d.mask + (size_t)y * d.pitch_k + off, npx, mw, kw);
+        uint32_t v = prev;
+        if (CONN == 8) {
+            uint32_t pw = __shfl_up_sync(FULL, prev, 1), nw = __shfl_down_sync(FULL, prev, 1);
+            if (lane == 0) pw = P::MINW;
+            if (lane == 31) nw = P::MINW;
+            v = P::vmax(v, P::vmax(P::shl1(prev, pw), P::shr1(prev, nw)));
+        }
+        const uint32_t x = P::vmax(mw, P::vmin(v, kw));
+        if (npx > 0 && x != mw) store_word_plain<DT>(mrow, npx, x);
+        prev = x;
+    }
+}
+
+// ------------------------------------------------------------ host side
+static unsigned blocks_for(long long threads, int block) {
+    long long b = (threads + block - 1) / block;
+    if (b < 1) b = 1;
+    if (b > (1ll << 30)) b = 1ll << 30;
+    return (unsigned)b;
+}
+
+cudaError_t launch_clip(const ImgDesc& d, cudaStream_t s) {
+    if (d.W == 0 || d.H == 0) return cudaSuccess;
+    const int ppw = d.dtype == DT_U8 ? 4 : d.dtype == DT_U16 ? 2 : 1;
+    const long long words = (long long)((d.W + ppw - 1) / ppw) * d.H;
+    unsigned blocks = blocks_for(words, 256);
+    if (blocks > 152u * 16u) blocks = 152u * 16u;
+    if (d.dtype == DT_U8)
+        clip_kernel<DT_U8><<<blocks, 256, 0, s>>>(d);
+    else if (d.dtype == DT_U16)
+        clip_kernel<DT_U16><<<blocks, 256, 0, s>>>(d);
+    else
+        clip_kernel<DT_I32><<<blocks, 256, 0, s>>>(d);
+    return cudaGetLastError();
+}
+
+template <int DT>
+static void launch_sweep_t(const ImgDesc& d, int direction, cudaStream_t s) {
+    using P = Px<DT>;
+    constexpr int TW = 32 * P::PPW;
+    if (direction == 0 || direction == 2) {
+        const unsigned blocks = blocks_for((long long)d.H * 32, 128);
+        if (direction == 0)
+            sweep_x_kernel<DT, true><<<blocks, 128, 0, s>>>(d);
+        else
+            sweep_x_kernel<DT, false><<<blocks, 128, 0, s>>>(d);
+    } else {
+        const int strips = (d.W + TW - 1) / TW;
+        const unsigned blocks = blocks_for((long long)strips * 32, 64);
+        const bool down = direction == 1;
+        if (d.conn == 8) {
+            if (down)
+                sweep_y_kernel<DT, 8, true><<<blocks, 64, 0, s>>>(d);
+            else
+                sweep_y_kernel<DT, 8, false><<<blocks, 64, 0, s>>>(d);
+        } else {
+            if (down)
+                sweep_y_kernel<DT, 4, true><<<blocks, 64, 0, s>>>(d);
+            else
+                sweep_y_kernel<DT, 4, false><<<blocks, 64, 0, s>>>(d);
+        }
+    }
+}
+
+cudaError_t launch_sweep(const ImgDesc& d, int direction, cudaStream_t s) {
+    if (d.W == 0 || d.H == 0) return cudaSuccess;
+    if (d.dtype == DT_U8)
+        launch_sweep_t<DT_U8>(d, direction, s);
+    else if (d.dtype == DT_U16)
+        launch_sweep_t<DT_U16>(d, direction, s);
+    else
+        launch_sweep_t<DT_I32>(d, direction, s);
+    return cudaGetLastError();
+}
+
+}  // namespace iwpp

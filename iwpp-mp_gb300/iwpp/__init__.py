@@ -1,0 +1,345 @@
+"""Host-side mirror of the reference's reconstruction interface over libiwpp.so.
+
+The reference exposes one synchronous C++ entry point per queue variant
+(``IWPP MP/include/MorphologicalReconstruction.cuh:45-46``)::
+
+    void MorphologicalReconstruction(unsigned char* marker, unsigned char* mask,
+                                     size_t pitchMarker, size_t pitchMask, int size);
+
+plus the ``clipImage`` precondition kernel (``MR.cu:827-836``) and
+``configureHeapSize`` (``IWPP MP/src/globalQueue.cu:3-6``).  This module binds
+the same names (raw device pointers, same argument meaning) and a general
+form over PyTorch CUDA tensors, which are only used as device buffers.  Every
+call goes through the C ABI in ``include/iwpp.h``; there is no CPU fallback:
+if the library is missing or no GB300 is present the call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from typing import Optional, Sequence
+
+from . import _build
+
+U8, U16, I32 = 0, 1, 2
+MUTEX, DOUBLE, UNIQUE, DEFAULT = 0, 1, 2, -1
+VARIANTS = {"mutex": MUTEX, "mp": MUTEX, "double": DOUBLE, "dq": DOUBLE, "unique": UNIQUE, "uq": UNIQUE,
+            "default": DEFAULT}
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "timeout", 4: "CUDA error",
+          5: "queue overflow restarts exhausted", 6: "no sm_103 device", 7: "busy"}
+
+
+class IwppError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        super().__init__(f"{what}: iwpp status {status} ({STATUS.get(status, '?')})")
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("tile_rows", ctypes.c_int), ("queue_capacity", ctypes.c_longlong),
+                ("init_passes", ctypes.c_int), ("grid_ctas", ctypes.c_int), ("max_restarts", ctypes.c_int),
+                ("timeout_ms", ctypes.c_int), ("clip_marker", ctypes.c_int)]
+
+    @classmethod
+    def make(cls, tile_rows=0, queue_capacity=0, init_passes=-1, grid_ctas=0, max_restarts=0, timeout_ms=0,
+             clip_marker=0):
+        return cls(tile_rows, queue_capacity, init_passes, grid_ctas, max_restarts, timeout_ms, clip_marker)
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("tiles", ctypes.c_longlong), ("visits", ctypes.c_longlong), ("sweeps", ctypes.c_longlong),
+                ("pushes", ctypes.c_longlong), ("rounds", ctypes.c_int), ("restarts", ctypes.c_int),
+                ("status", ctypes.c_int), ("variant", ctypes.c_int), ("device_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Image(ctypes.Structure):
+    _fields_ = [("marker", ctypes.c_void_p), ("mask", ctypes.c_void_p), ("pitch_marker", ctypes.c_size_t),
+                ("pitch_mask", ctypes.c_size_t), ("width", ctypes.c_int), ("height", ctypes.c_int),
+                ("dtype", ctypes.c_int), ("connectivity", ctypes.c_int)]
+
+
+# Every symbol include/iwpp.h declares, with its ctypes signature.
+_SIGS = {
+    "iwpp_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "iwpp_version": (ctypes.c_int, []),
+    "iwpp_handle_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
+    "iwpp_handle_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "iwpp_workspace_bytes": (ctypes.c_longlong, [ctypes.c_longlong, ctypes.c_int, ctypes.c_longlong]),
+    "iwpp_tile_count": (ctypes.c_longlong, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "iwpp_reconstruct": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                        ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, ctypes.POINTER(Config), ctypes.c_void_p,
+                                        ctypes.POINTER(Stats)]),
+    "iwpp_reconstruct_async": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                              ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                              ctypes.c_int, ctypes.c_int, ctypes.POINTER(Config),
+                                              ctypes.c_void_p]),
+    "iwpp_handle_sync": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)]),
+    "iwpp_reconstruct_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Image), ctypes.c_int, ctypes.c_int,
+                                              ctypes.POINTER(Config), ctypes.c_void_p, ctypes.POINTER(Stats)]),
+    "iwpp_plan_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_void_p, ctypes.POINTER(Image),
+                                        ctypes.c_int, ctypes.c_int, ctypes.POINTER(Config)]),
+    "iwpp_plan_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "iwpp_plan_sync": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)]),
+    "iwpp_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "iwpp_clip": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int,
+                                 ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
+    "iwpp_sweep": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int,
+                                  ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
+    "iwpp_sweep_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_float)]),
+    "MorphologicalReconstruction": (None, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
+                                           ctypes.c_int]),
+    "configureHeapSize": (None, []),
+    "iwpp_last_status": (ctypes.c_int, []),
+}
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def library_path() -> str:
+    return _build.LIBIWPP
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Loads libiwpp.so (building it first if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIBIWPP
+    if build_if_missing:
+        _build.build_iwpp()
+    if not os.path.exists(path):
+        raise ImportError(f"libiwpp.so not built at {path}")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGS)
+
+
+def status_string(status: int) -> str:
+    return load().iwpp_status_string(status).decode()
+
+
+# ----------------------------------------------------------------- helpers
+def _torch():
+    import torch
+    return torch
+
+
+def dtype_code(t) -> int:
+    torch = _torch()
+    if t.dtype == torch.uint8:
+        return U8
+    if getattr(torch, "uint16", None) is not None and t.dtype == torch.uint16:
+        return U16
+    if t.dtype == torch.int16:  # raw 16-bit storage holding unsigned values
+        return U16
+    if t.dtype == torch.int32:
+        return I32
+    raise TypeError(f"unsupported pixel dtype {t.dtype}")
+
+
+def _pitch(t) -> int:
+    if t.dim() != 2 or t.stride(1) != 1:
+        raise ValueError("images must be 2-D with unit column stride")
+    return t.stride(0) * t.element_size()
+
+
+def _check_cuda(t, name):
+    if not t.is_cuda:
+        raise ValueError(f"{name} must be a CUDA tensor (device memory)")
+
+
+def _variant(v) -> int:
+    if isinstance(v, str):
+        return VARIANTS[v.lower()]
+    return int(v)
+
+
+def _stream_ptr(stream) -> Optional[int]:
+    if stream is None:
+        torch = _torch()
+        return torch.cuda.current_stream().cuda_stream
+    return getattr(stream, "cuda_stream", stream)
+
+
+# ----------------------------------------------- reference-compatible names
+def MorphologicalReconstruction(marker_ptr: int, mask_ptr: int, pitchMarker: int, pitchMask: int, size: int) -> None:
+    """Exactly the reference entry point: uint8, size x size, 4-connected,
+    synchronous, in place on the device buffer at ``marker_ptr``."""
+    lib = load()
+    lib.MorphologicalReconstruction(marker_ptr, mask_ptr, pitchMarker, pitchMask, size)
+    st = lib.iwpp_last_status()
+    if st != 0:
+        raise IwppError(st, "MorphologicalReconstruction")
+
+
+def clipImage(marker_ptr: int, mask_ptr: int, pitchMarker: int, pitchMask: int, size: int) -> None:
+    """The reference's precondition kernel (marker = min(marker, mask)) for a
+    size x size uint8 image, on the default stream."""
+    lib = load()
+    st = lib.iwpp_clip(marker_ptr, mask_ptr, pitchMarker, pitchMask, size, size, U8, None)
+    if st != 0:
+        raise IwppError(st, "clipImage")
+
+
+def configureHeapSize() -> None:
+    load().configureHeapSize()
+
+
+# ------------------------------------------------------------ general API
+class Handle:
+    """Owns a device workspace; calls through one handle are stream-ordered."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load()
+        h = ctypes.c_void_p()
+        st = self._lib.iwpp_handle_create(ctypes.byref(h), device)
+        if st != 0:
+            raise IwppError(st, "iwpp_handle_create")
+        self.ptr = h
+
+    def close(self):
+        if self.ptr:
+            self._lib.iwpp_handle_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def reconstruct(marker, mask, connectivity: int = 8, variant="default", config: Optional[Config] = None,
+                stream=None, handle: Optional[Handle] = None, check: bool = True) -> Stats:
+    """In-place reconstruction by dilation of ``marker`` under ``mask`` (2-D CUDA
+    tensors of uint8 / uint16 (or int16 storage) / int32).  Synchronous."""
+    lib = load()
+    _check_cuda(marker, "marker")
+    _check_cuda(mask, "mask")
+    if marker.shape != mask.shape or marker.dtype != mask.dtype:
+        raise ValueError("marker and mask must have the same shape and dtype")
+    h, w = marker.shape
+    stats = Stats()
+    st = lib.iwpp_reconstruct(handle.ptr if handle else None, marker.data_ptr(), mask.data_ptr(), _pitch(marker),
+                              _pitch(mask), w, h, dtype_code(marker), connectivity, _variant(variant),
+                              ctypes.byref(config) if config is not None else None, _stream_ptr(stream),
+                              ctypes.byref(stats))
+    if check and st != 0:
+        raise IwppError(st, "iwpp_reconstruct")
+    stats.status = st
+    return stats
+
+
+def reconstruct_batch(pairs: Sequence, connectivity=None, variant="default", config: Optional[Config] = None,
+                      stream=None, handle: Optional[Handle] = None, check: bool = True) -> Stats:
+    """All (marker, mask[, connectivity]) pairs in one persistent launch."""
+    lib = load()
+    arr = (Image * max(len(pairs), 1))()
+    for i, p in enumerate(pairs):
+        m, k = p[0], p[1]
+        conn = p[2] if len(p) > 2 else (connectivity or 8)
+        _check_cuda(m, "marker")
+        _check_cuda(k, "mask")
+        arr[i] = Image(m.data_ptr(), k.data_ptr(), _pitch(m), _pitch(k), m.shape[1], m.shape[0], dtype_code(m), conn)
+    stats = Stats()
+    st = lib.iwpp_reconstruct_batch(handle.ptr if handle else None, arr, len(pairs), _variant(variant),
+                                    ctypes.byref(config) if config is not None else None, _stream_ptr(stream),
+                                    ctypes.byref(stats))
+    if check and st != 0:
+        raise IwppError(st, "iwpp_reconstruct_batch")
+    stats.status = st
+    return stats
+
+
+class Plan:
+    """A batch captured once into a CUDA graph; launch() re-runs it."""
+
+    def __init__(self, handle: Handle, pairs: Sequence, variant="default", config: Optional[Config] = None):
+        self._lib = load()
+        self.handle = handle
+        self._keep = list(pairs)
+        arr = (Image * max(len(pairs), 1))()
+        for i, p in enumerate(pairs):
+            m, k = p[0], p[1]
+            conn = p[2] if len(p) > 2 else 8
+            arr[i] = Image(m.data_ptr(), k.data_ptr(), _pitch(m), _pitch(k), m.shape[1], m.shape[0], dtype_code(m),
+                           conn)
+        ptr = ctypes.c_void_p()
+        st = self._lib.iwpp_plan_create(ctypes.byref(ptr), handle.ptr, arr, len(pairs), _variant(variant),
+                                        ctypes.byref(config) if config is not None else None)
+        if st != 0:
+            raise IwppError(st, "iwpp_plan_create")
+        self.ptr = ptr
+
+    def launch(self, stream=None):
+        st = self._lib.iwpp_plan_launch(self.ptr, _stream_ptr(stream))
+        if st != 0:
+            raise IwppError(st, "iwpp_plan_launch")
+
+    def sync(self) -> Stats:
+        stats = Stats()
+        st = self._lib.iwpp_plan_sync(self.ptr, ctypes.byref(stats))
+        if st != 0:
+            raise IwppError(st, "iwpp_plan_sync")
+        return stats
+
+    def close(self):
+        if self.ptr:
+            self._lib.iwpp_plan_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def clip(marker, mask, stream=None) -> None:
+    lib = load()
+    h, w = marker.shape
+    st = lib.iwpp_clip(marker.data_ptr(), mask.data_ptr(), _pitch(marker), _pitch(mask), w, h, dtype_code(marker),
+                       _stream_ptr(stream))
+    if st != 0:
+        raise IwppError(st, "iwpp_clip")
+
+
+def sweep(marker, mask, direction: int, connectivity: int = 8, stream=None) -> None:
+    """One whole-image sweep: 0 = +X, 1 = +Y, 2 = -X, 3 = -Y."""
+    lib = load()
+    h, w = marker.shape
+    st = lib.iwpp_sweep(marker.data_ptr(), mask.data_ptr(), _pitch(marker), _pitch(mask), w, h, dtype_code(marker),
+                        connectivity, direction, _stream_ptr(stream))
+    if st != 0:
+        raise IwppError(st, "iwpp_sweep")
+
+
+def sweep_timing(marker, mask, connectivity: int = 8) -> list[float]:
+    lib = load()
+    h, w = marker.shape
+    out = (ctypes.c_float * 4)()
+    st = lib.iwpp_sweep_timing(marker.data_ptr(), mask.data_ptr(), _pitch(marker), _pitch(mask), w, h,
+                               dtype_code(marker), connectivity, out)
+    if st != 0:
+        raise IwppError(st, "iwpp_sweep_timing")
+    return list(out)
+
+
+def tile_count(width: int, height: int, dtype: int, tile_rows: int = 0) -> int:
+    return int(load().iwpp_tile_count(width, height, dtype, tile_rows))

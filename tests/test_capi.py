@@ -1,0 +1,97 @@
+"""The C-ABI library: it loads, exports every symbol include/iwpp.h declares,
+and its host-only functions behave (no GPU needed)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+import iwpp
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(REPO, "include", "iwpp.h")
+
+
+def _declared():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"IWPP_API\s+[\w\s\*]+?\b(\w+)\s*\(", text)))
+
+
+def test_header_declarations_parsed():
+    names = _declared()
+    assert "iwpp_reconstruct" in names and "MorphologicalReconstruction" in names
+    assert len(names) >= 20
+
+
+def test_library_exports_every_declared_symbol():
+    lib = iwpp.load()
+    out = subprocess.run(["nm", "-D", "--defined-only", iwpp.library_path()], stdout=subprocess.PIPE, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if line.strip()}
+    for name in _declared():
+        assert name in exported, name
+        getattr(lib, name)  # resolvable through ctypes too
+    # the Python binding covers exactly the declared surface
+    assert sorted(iwpp.exported_symbols()) == _declared()
+
+
+def test_library_exports_nothing_else():
+    out = subprocess.run(["nm", "-D", "--defined-only", iwpp.library_path()], stdout=subprocess.PIPE, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if line.strip()}
+    ours = {n for n in exported if not n.startswith("_")}
+    assert ours == set(_declared())
+
+
+def test_status_strings_and_version():
+    lib = iwpp.load()
+    assert lib.iwpp_version() == 1
+    assert lib.iwpp_status_string(0) == b"ok"
+    assert b"timed out" in lib.iwpp_status_string(3)
+    assert lib.iwpp_status_string(99) == b"unknown status"
+
+
+def test_tile_counts():
+    lib = iwpp.load()
+    # tiles are 128 bytes wide: 128 uint8, 64 uint16, 32 int32 pixels
+    assert lib.iwpp_tile_count(4096, 4096, 0, 64) == 32 * 64
+    assert lib.iwpp_tile_count(4096, 4096, 1, 64) == 64 * 64
+    assert lib.iwpp_tile_count(4096, 4096, 2, 32) == 128 * 128
+    assert lib.iwpp_tile_count(129, 65, 0, 64) == 2 * 2
+    assert lib.iwpp_tile_count(0, 10, 0, 64) == 0
+    assert lib.iwpp_tile_count(10, 10, 7, 64) == -1
+
+
+def test_workspace_bytes_grow_with_tiles():
+    lib = iwpp.load()
+    a = lib.iwpp_workspace_bytes(1000, 2, 0)
+    b = lib.iwpp_workspace_bytes(100000, 2, 0)
+    assert 0 < a < b
+    # the double queue keeps two buffers, the mutex stack one
+    assert lib.iwpp_workspace_bytes(100000, 1, 0) > lib.iwpp_workspace_bytes(100000, 0, 0)
+
+
+def test_invalid_arguments_rejected_before_any_device_work():
+    lib = iwpp.load()
+    st = iwpp.Stats()
+    # bad connectivity, bad dtype, pitch too small, negative size
+    assert lib.iwpp_reconstruct(None, 16, 16, 64, 64, 64, 64, 0, 6, 2, None, None, ctypes.byref(st)) == 1
+    assert lib.iwpp_reconstruct(None, 16, 16, 64, 64, 64, 64, 9, 8, 2, None, None, ctypes.byref(st)) == 1
+    assert lib.iwpp_reconstruct(None, 16, 16, 32, 64, 64, 64, 0, 8, 2, None, None, ctypes.byref(st)) == 1
+    assert lib.iwpp_reconstruct(None, 16, 16, 64, 64, -1, 64, 0, 8, 2, None, None, ctypes.byref(st)) == 1
+    assert lib.iwpp_reconstruct(None, None, None, 64, 64, 64, 64, 0, 8, 2, None, None, ctypes.byref(st)) == 1
+    assert lib.iwpp_last_status() == 1
+
+
+def test_no_device_reported_without_gpu():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    lib = iwpp.load()
+    h = ctypes.c_void_p()
+    assert lib.iwpp_handle_create(ctypes.byref(h), 0) == 6
+    # a valid empty image needs no device at all
+    st = iwpp.Stats()
+    assert lib.iwpp_reconstruct(None, None, None, 0, 0, 0, 0, 0, 8, 2, None, None, ctypes.byref(st)) == 0
