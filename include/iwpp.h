@@ -54,6 +54,8 @@ typedef struct iwpp_config {
     int max_restarts;          /* queue-overflow restarts allowed; 0 = default (64) */
     int timeout_ms;            /* bound on every device-side wait; 0 = default (10000) */
     int clip_marker;           /* 1: marker = min(marker, mask) before reconstructing */
+    int plain_loads;           /* 1: never use TMA box loads (else TMA whenever base and
+                                  pitch are 16-byte aligned) */
 } iwpp_config;
 
 typedef struct iwpp_stats {

@@ -11,6 +11,9 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "iwpp.h"
 #include "iwpp_engine.cuh"
 
@@ -53,6 +56,7 @@ struct Config {
     int max_restarts;
     int timeout_ms;
     int clip_marker;
+    int plain_loads;
 };
 
 Config resolve_config(const iwpp_config* c) {
@@ -64,7 +68,43 @@ Config resolve_config(const iwpp_config* c) {
     r.max_restarts = c && c->max_restarts > 0 ? c->max_restarts : 64;
     r.timeout_ms = c && c->timeout_ms > 0 ? c->timeout_ms : 10000;
     r.clip_marker = c ? c->clip_marker : 0;
+    r.plain_loads = c ? c->plain_loads : 0;
+    if (std::getenv("IWPP_PLAIN_LOADS")) r.plain_loads = 1;
     return r;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no
+// libcuda link needed).
+PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        cudaGetLastError();
+    });
+    return fn;
+}
+
+// A 2-D map over the image's bytes (uint8 elements): dims {W * bpp, H},
+// row pitch in bytes, box {128 bytes, TH + 2 rows}.  Needs 16-byte aligned
+// base and pitch.
+bool encode_tmap(CUtensorMap* out, const void* base, int w, int h, size_t pitch, int bpp, int th) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
+    if (!enc) return false;
+    if ((reinterpret_cast<uintptr_t>(base) & 15u) != 0u || (pitch & 15u) != 0u) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)w * (cuuint64_t)bpp, (cuuint64_t)h};
+    cuuint64_t strides[1] = {(cuuint64_t)pitch};
+    cuuint32_t box[2] = {128u, (cuuint32_t)(th + 2)};
+    cuuint32_t estr[2] = {1u, 1u};
+    CUresult r = enc(out, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(base), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
 }
 
 bool aligned_for_engine(const void* p, size_t pitch) {
@@ -107,13 +147,14 @@ struct Workspace {
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 struct Layout {
-    size_t off_imgs, off_state, off_q0, off_q1, total;
+    size_t off_imgs, off_tmaps, off_state, off_q0, off_q1, total;
 };
 
 Layout layout_for(long long n_imgs, long long G, long long cap, bool two_queues) {
     Layout l;
     l.off_imgs = align_up(sizeof(Ctrl), 256);
-    l.off_state = align_up(l.off_imgs + (size_t)n_imgs * sizeof(ImgDesc), 256);
+    l.off_tmaps = align_up(l.off_imgs + (size_t)n_imgs * sizeof(ImgDesc), 256);
+    l.off_state = align_up(l.off_tmaps + (size_t)n_imgs * 2u * sizeof(CUtensorMap), 256);
     l.off_q0 = align_up(l.off_state + (size_t)G * 4u, 256);
     l.off_q1 = align_up(l.off_q0 + (size_t)cap * 4u, 256);
     l.total = align_up(l.off_q1 + (two_queues ? (size_t)cap * 4u : 0u), 256);
@@ -145,6 +186,8 @@ struct Staged {
 struct Job {
     std::vector<ImgDesc> descs;
     std::vector<Staged> staged;
+    std::vector<CUtensorMap> tmaps;  // two per descriptor (marker, mask)
+    std::vector<char> has_tma;
     long long G = 0;
     int tile_rows = 64;
     int variant = IWPP_QUEUE_UNIQUE;
@@ -212,6 +255,14 @@ int build_job(Job& job, const iwpp_image* imgs, int n, int variant, const iwpp_c
         }
         G += (long long)d.tiles_x * d.tiles_y;
         if (G > 0x7fffffffll) return IWPP_ERR_INVALID;
+        CUtensorMap maps[2];
+        std::memset(maps, 0, sizeof(maps));
+        bool tma = !job.cfg.plain_loads &&
+                   encode_tmap(&maps[0], d.marker, d.W, d.H, (size_t)d.pitch_m, bpp_of(d.dtype), th) &&
+                   encode_tmap(&maps[1], d.mask, d.W, d.H, (size_t)d.pitch_k, bpp_of(d.dtype), th);
+        job.tmaps.push_back(maps[0]);
+        job.tmaps.push_back(maps[1]);
+        job.has_tma.push_back(tma ? 1 : 0);
         job.descs.push_back(d);
         job.staged.push_back(st);
     }
@@ -315,9 +366,16 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
     a.max_restarts = job.cfg.max_restarts;
 
     cudaError_t e = cudaSuccess;
-    if (upload_descs && !job.descs.empty())
-        e = cudaMemcpyAsync(base + l.off_imgs, job.descs.data(), job.descs.size() * sizeof(ImgDesc),
+    if (upload_descs && !job.descs.empty()) {
+        std::vector<ImgDesc> descs = job.descs;
+        for (size_t i = 0; i < descs.size(); ++i)
+            descs[i].tmaps = job.has_tma[i] ? base + l.off_tmaps + i * 2u * sizeof(CUtensorMap) : nullptr;
+        e = cudaMemcpyAsync(base + l.off_tmaps, job.tmaps.data(), job.tmaps.size() * sizeof(CUtensorMap),
                             cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(base + l.off_imgs, descs.data(), descs.size() * sizeof(ImgDesc),
+                                cudaMemcpyHostToDevice, s);
+    }
     if (e != cudaSuccess) return cuda_status(e);
     if (use_events) cudaEventRecord(ev0, s);
     if (job.cfg.clip_marker)
@@ -606,8 +664,15 @@ int iwpp_plan_create(iwpp_plan* out, iwpp_handle h, const iwpp_image* images, in
         const Layout l = layout_for((long long)job.descs.size(), job.G, cap, two);
         rc = ensure_workspace(p->ws, l.total);
         if (rc == IWPP_OK && !job.descs.empty()) {
-            e = cudaMemcpy(static_cast<char*>(p->ws.base) + l.off_imgs, job.descs.data(),
-                           job.descs.size() * sizeof(ImgDesc), cudaMemcpyHostToDevice);
+            char* wbase = static_cast<char*>(p->ws.base);
+            std::vector<ImgDesc> descs = job.descs;
+            for (size_t i = 0; i < descs.size(); ++i)
+                descs[i].tmaps = job.has_tma[i] ? wbase + l.off_tmaps + i * 2u * sizeof(CUtensorMap) : nullptr;
+            e = cudaMemcpy(wbase + l.off_tmaps, job.tmaps.data(), job.tmaps.size() * sizeof(CUtensorMap),
+                           cudaMemcpyHostToDevice);
+            if (e == cudaSuccess)
+                e = cudaMemcpy(wbase + l.off_imgs, descs.data(), descs.size() * sizeof(ImgDesc),
+                               cudaMemcpyHostToDevice);
             rc = cuda_status(e);
         }
         // Warm the kernel attributes before capture.

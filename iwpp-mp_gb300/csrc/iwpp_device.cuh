@@ -1,13 +1,16 @@
 // iwpp_device.cuh -- device building blocks of the GB300 reconstruction
-// engine: packed-pixel arithmetic, one-warp tile visits (load, raster /
-// anti-raster sweeps to local convergence, write-back, neighbour detection).
+// engine: one-warp tile visits (TMA fetch with halo, raster / anti-raster
+// sweeps to local convergence, write-back, neighbour detection).
 //
 // Layout: a tile is TH rows x TW pixels with TW * sizeof(pixel) = 128 bytes
-// (TW = 128 uint8, 64 uint16, 32 int32).  One warp owns one tile at a time;
-// lane L keeps the 32-bit word holding pixels [L*PPW, L*PPW + PPW) of every
-// row in registers (PPW = pixels per word = 4 / 2 / 1), for both marker and
-// mask.  Vertical propagation is therefore register-serial inside a lane and
-// horizontal propagation is a warp scan over the max-min semiring.
+// (TW = 128 uint8, 64 uint16, 32 int32).  One warp owns one tile at a time.
+// Shared memory holds the tile plus the halo rows above and below as dense
+// 128-byte rows (SMEM row r = image row y0 - 1 + r), so one TMA box load per
+// image plane fetches it.  Lane L owns the 32-bit word with pixels
+// [L*PPW, L*PPW + PPW) of every row (PPW = 4 / 2 / 1); during a row step it
+// unpacks them to one pixel per register so every min / max is a native
+// 32-bit instruction.  Vertical propagation runs row by row; horizontal
+// propagation is a warp scan over the max-min semiring.
 //
 // Reference counterparts (IWPP MP/src/MorphologicalReconstruction.cu):
 //   tile fetch with a one-pixel halo        MR.cu:232-312
@@ -25,7 +28,9 @@ constexpr unsigned FULL = 0xffffffffu;
 
 enum : int { DT_U8 = 0, DT_U16 = 1, DT_I32 = 2 };
 
-// --------------------------------------------------------------- pixel words
+// ------------------------------------------------------------------ pixels
+// Pixels are carried as uint32 (zero-extended for the unsigned types, the
+// bit pattern for int32); Px<DT> supplies the order and the packing.
 template <int DT>
 struct Px;
 
@@ -35,44 +40,23 @@ struct Px<DT_U8> {
     static constexpr int BPP = 1;
     static constexpr uint32_t MINPX = 0u;
     static constexpr uint32_t MINW = 0u;
-    __device__ static __forceinline__ uint32_t vmax(uint32_t a, uint32_t b) { return __vmaxu4(a, b); }
-    __device__ static __forceinline__ uint32_t vmin(uint32_t a, uint32_t b) { return __vminu4(a, b); }
-    __device__ static __forceinline__ bool any_gt(uint32_t a, uint32_t b) { return __vcmpgtu4(a, b) != 0u; }
-    __device__ static __forceinline__ uint32_t smax(uint32_t a, uint32_t b) { return a > b ? a : b; }
-    __device__ static __forceinline__ uint32_t smin(uint32_t a, uint32_t b) { return a < b ? a : b; }
+    __device__ static __forceinline__ uint32_t mx(uint32_t a, uint32_t b) { return max(a, b); }
+    __device__ static __forceinline__ uint32_t mn(uint32_t a, uint32_t b) { return min(a, b); }
+    __device__ static __forceinline__ uint32_t mx3(uint32_t a, uint32_t b, uint32_t c) { return __vimax3_u32(a, b, c); }
     __device__ static __forceinline__ bool gt(uint32_t a, uint32_t b) { return a > b; }
-    __device__ static __forceinline__ uint32_t first(uint32_t w) { return w & 0xffu; }
-    __device__ static __forceinline__ uint32_t last(uint32_t w) { return w >> 24; }
-    __device__ static __forceinline__ uint32_t as_last(uint32_t px) { return px << 24; }
-    __device__ static __forceinline__ uint32_t bcast(uint32_t px) { return px * 0x01010101u; }
-    // pixel i <- pixel i-1 (pixel 0 <- last pixel of `prev`)
-    __device__ static __forceinline__ uint32_t shl1(uint32_t w, uint32_t prev) { return __funnelshift_l(prev, w, 8); }
-    // pixel i <- pixel i+1 (last pixel <- first pixel of `next`)
-    __device__ static __forceinline__ uint32_t shr1(uint32_t w, uint32_t next) { return __funnelshift_r(w, next, 8); }
-    __device__ static __forceinline__ uint32_t hmin(uint32_t w) {
-        uint32_t t = vmin(w, __funnelshift_r(w, w, 8));
-        t = vmin(t, __funnelshift_r(t, t, 16));
-        return t & 0xffu;
+    __device__ static __forceinline__ void unpack(uint32_t w, uint32_t (&p)[4]) {
+        p[0] = __byte_perm(w, 0u, 0x4440);
+        p[1] = __byte_perm(w, 0u, 0x4441);
+        p[2] = __byte_perm(w, 0u, 0x4442);
+        p[3] = __byte_perm(w, 0u, 0x4443);
     }
-    // prefix (forward) or suffix (backward) minimum of the pixels of a word
-    template <bool FWD>
-    __device__ static __forceinline__ uint32_t scanmin(uint32_t w) {
-        if (FWD) {
-            w = vmin(w, (w << 8) | 0x000000ffu);
-            return vmin(w, (w << 16) | 0x0000ffffu);
-        } else {
-            w = vmin(w, (w >> 8) | 0xff000000u);
-            return vmin(w, (w >> 16) | 0xffff0000u);
-        }
+    __device__ static __forceinline__ uint32_t pack(const uint32_t (&p)[4]) {
+        const uint32_t lo = __byte_perm(p[0], p[1], 0x0040);
+        const uint32_t hi = __byte_perm(p[2], p[3], 0x0040);
+        return __byte_perm(lo, hi, 0x5410);
     }
-    __device__ static __forceinline__ uint32_t pack2(uint32_t a, uint32_t b) { return a | (b << 16); }
-    __device__ static __forceinline__ uint32_t unpack_a(uint32_t p) { return p & 0xffffu; }
-    __device__ static __forceinline__ uint32_t unpack_b(uint32_t p) { return p >> 16; }
-    __device__ static __forceinline__ uint32_t get(uint32_t w, int i) { return (w >> (8 * i)) & 0xffu; }
     __device__ static __forceinline__ uint32_t ld_px(const unsigned char* p) { return *p; }
-    __device__ static __forceinline__ uint32_t ld_px_cg(const unsigned char* p) {
-        return __ldcg(reinterpret_cast<const unsigned char*>(p));
-    }
+    __device__ static __forceinline__ uint32_t ld_px_cg(const unsigned char* p) { return __ldcg(p); }
     __device__ static __forceinline__ void st_px(unsigned char* p, uint32_t v) { *p = (unsigned char)v; }
 };
 
@@ -82,27 +66,15 @@ struct Px<DT_U16> {
     static constexpr int BPP = 2;
     static constexpr uint32_t MINPX = 0u;
     static constexpr uint32_t MINW = 0u;
-    __device__ static __forceinline__ uint32_t vmax(uint32_t a, uint32_t b) { return __vmaxu2(a, b); }
-    __device__ static __forceinline__ uint32_t vmin(uint32_t a, uint32_t b) { return __vminu2(a, b); }
-    __device__ static __forceinline__ bool any_gt(uint32_t a, uint32_t b) { return __vcmpgtu2(a, b) != 0u; }
-    __device__ static __forceinline__ uint32_t smax(uint32_t a, uint32_t b) { return a > b ? a : b; }
-    __device__ static __forceinline__ uint32_t smin(uint32_t a, uint32_t b) { return a < b ? a : b; }
+    __device__ static __forceinline__ uint32_t mx(uint32_t a, uint32_t b) { return max(a, b); }
+    __device__ static __forceinline__ uint32_t mn(uint32_t a, uint32_t b) { return min(a, b); }
+    __device__ static __forceinline__ uint32_t mx3(uint32_t a, uint32_t b, uint32_t c) { return __vimax3_u32(a, b, c); }
     __device__ static __forceinline__ bool gt(uint32_t a, uint32_t b) { return a > b; }
-    __device__ static __forceinline__ uint32_t first(uint32_t w) { return w & 0xffffu; }
-    __device__ static __forceinline__ uint32_t last(uint32_t w) { return w >> 16; }
-    __device__ static __forceinline__ uint32_t as_last(uint32_t px) { return px << 16; }
-    __device__ static __forceinline__ uint32_t bcast(uint32_t px) { return px | (px << 16); }
-    __device__ static __forceinline__ uint32_t shl1(uint32_t w, uint32_t prev) { return __funnelshift_l(prev, w, 16); }
-    __device__ static __forceinline__ uint32_t shr1(uint32_t w, uint32_t next) { return __funnelshift_r(w, next, 16); }
-    __device__ static __forceinline__ uint32_t hmin(uint32_t w) { return vmin(w, __funnelshift_r(w, w, 16)) & 0xffffu; }
-    template <bool FWD>
-    __device__ static __forceinline__ uint32_t scanmin(uint32_t w) {
-        return FWD ? vmin(w, (w << 16) | 0x0000ffffu) : vmin(w, (w >> 16) | 0xffff0000u);
+    __device__ static __forceinline__ void unpack(uint32_t w, uint32_t (&p)[2]) {
+        p[0] = w & 0xffffu;
+        p[1] = w >> 16;
     }
-    __device__ static __forceinline__ uint32_t pack2(uint32_t a, uint32_t b) { return a | (b << 16); }
-    __device__ static __forceinline__ uint32_t unpack_a(uint32_t p) { return p & 0xffffu; }
-    __device__ static __forceinline__ uint32_t unpack_b(uint32_t p) { return p >> 16; }
-    __device__ static __forceinline__ uint32_t get(uint32_t w, int i) { return (w >> (16 * i)) & 0xffffu; }
+    __device__ static __forceinline__ uint32_t pack(const uint32_t (&p)[2]) { return __byte_perm(p[0], p[1], 0x5410); }
     __device__ static __forceinline__ uint32_t ld_px(const unsigned char* p) {
         return *reinterpret_cast<const unsigned short*>(p);
     }
@@ -120,22 +92,14 @@ struct Px<DT_I32> {
     static constexpr int BPP = 4;
     static constexpr uint32_t MINPX = 0x80000000u;
     static constexpr uint32_t MINW = 0x80000000u;
-    __device__ static __forceinline__ uint32_t vmax(uint32_t a, uint32_t b) { return (uint32_t)max((int)a, (int)b); }
-    __device__ static __forceinline__ uint32_t vmin(uint32_t a, uint32_t b) { return (uint32_t)min((int)a, (int)b); }
-    __device__ static __forceinline__ bool any_gt(uint32_t a, uint32_t b) { return (int)a > (int)b; }
-    __device__ static __forceinline__ uint32_t smax(uint32_t a, uint32_t b) { return vmax(a, b); }
-    __device__ static __forceinline__ uint32_t smin(uint32_t a, uint32_t b) { return vmin(a, b); }
+    __device__ static __forceinline__ uint32_t mx(uint32_t a, uint32_t b) { return (uint32_t)max((int)a, (int)b); }
+    __device__ static __forceinline__ uint32_t mn(uint32_t a, uint32_t b) { return (uint32_t)min((int)a, (int)b); }
+    __device__ static __forceinline__ uint32_t mx3(uint32_t a, uint32_t b, uint32_t c) {
+        return (uint32_t)__vimax3_s32((int)a, (int)b, (int)c);
+    }
     __device__ static __forceinline__ bool gt(uint32_t a, uint32_t b) { return (int)a > (int)b; }
-    __device__ static __forceinline__ uint32_t first(uint32_t w) { return w; }
-    __device__ static __forceinline__ uint32_t last(uint32_t w) { return w; }
-    __device__ static __forceinline__ uint32_t as_last(uint32_t px) { return px; }
-    __device__ static __forceinline__ uint32_t bcast(uint32_t px) { return px; }
-    __device__ static __forceinline__ uint32_t shl1(uint32_t, uint32_t prev) { return prev; }
-    __device__ static __forceinline__ uint32_t shr1(uint32_t, uint32_t next) { return next; }
-    __device__ static __forceinline__ uint32_t hmin(uint32_t w) { return w; }
-    template <bool FWD>
-    __device__ static __forceinline__ uint32_t scanmin(uint32_t w) { return w; }
-    __device__ static __forceinline__ uint32_t get(uint32_t w, int) { return w; }
+    __device__ static __forceinline__ void unpack(uint32_t w, uint32_t (&p)[1]) { p[0] = w; }
+    __device__ static __forceinline__ uint32_t pack(const uint32_t (&p)[1]) { return p[0]; }
     __device__ static __forceinline__ uint32_t ld_px(const unsigned char* p) {
         return (uint32_t)*reinterpret_cast<const int*>(p);
     }
@@ -152,6 +116,7 @@ struct ImgDesc {
     const unsigned char* mask;
     long long pitch_m;
     long long pitch_k;
+    const void* tmaps;  // two CUtensorMap (marker, mask) or nullptr (plain loads)
     int W, H;
     int dtype, conn;
     int tiles_x, tiles_y;
@@ -167,47 +132,97 @@ enum : unsigned {
 __device__ __constant__ static const int kNbDx[8] = {0, 0, -1, 1, -1, 1, -1, 1};
 __device__ __constant__ static const int kNbDy[8] = {-1, 1, 0, 0, -1, -1, 1, 1};
 
-// Per-warp shared memory: the tile's marker and mask words (row stride 33
-// words so that a row is conflict-free for the 32 lanes and so is a column),
-// and the left / right halo columns, where index i holds row i-1 (index 0 is
-// the row above the tile, index TH+1 the row below).
-constexpr int kRowStride = 33;
-
+// Per-warp shared memory (128-byte aligned; TMA writes tm / tk densely).
+// SMEM row r holds image row y0 - 1 + r: row 0 is the halo above the tile,
+// rows 1..TH the tile, row TH+1 the halo below.  hL* / hR* hold the left /
+// right halo column pixels of the same rows.
 template <int TH>
-struct WarpSmem {
-    uint32_t tm[TH * kRowStride];
-    uint32_t tk[TH * kRowStride];
+struct __align__(128) WarpSmem {
+    uint32_t tm[(TH + 2) * 32];
+    uint32_t tk[(TH + 2) * 32];
     uint32_t hLm[TH + 2];
     uint32_t hLk[TH + 2];
     uint32_t hRm[TH + 2];
     uint32_t hRk[TH + 2];
+    unsigned long long mbar;
 };
 
+// ------------------------------------------------------- async-copy helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0u;
+}
+
+// 2-D TMA box load: box origin (x bytes, y rows) of the tensor map into smem.
+__device__ __forceinline__ void tma_load_2d(void* smem_dst, const void* tmap, int x, int y,
+                                            unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(smem_u32(smem_dst)),
+        "l"(tmap), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+
+__device__ __forceinline__ long long globaltimer_ns() {
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // ---------------------------------------------------- horizontal warp scan
-// Propagates along one row in scan order (FWD: left to right), with `cin` the
+// Propagates along one row in scan order (FWD: left to right) with `cin` the
 // marker value of the halo pixel entering the row at the first lane.  The
-// per-word transfer function of x (the value entering a word) is
-// f(x) = max(min(x, B), A) with B = min of the word's mask pixels and A = the
-// word's exit pixel after the intra-word pass; these compose associatively:
+// transfer function of a word for the value x entering it is
+// f(x) = max(min(x, B), A) with B = min of its mask pixels and A = its exit
+// pixel after the in-word pass; these compose associatively:
 // (A2,B2) o (A1,B1) = (max(min(A1, B2), A2), min(B1, B2)).
 template <int DT, bool FWD>
-__device__ __forceinline__ uint32_t hscan(uint32_t m, uint32_t k, uint32_t cin, int lane) {
+__device__ __forceinline__ void hscan(uint32_t (&m)[Px<DT>::PPW], const uint32_t (&k)[Px<DT>::PPW], uint32_t cin,
+                                      int lane) {
     using P = Px<DT>;
+    constexpr int N = P::PPW;
 #pragma unroll
-    for (int s = 1; s < P::PPW; ++s) m = P::vmax(m, P::vmin(FWD ? P::shl1(m, P::MINW) : P::shr1(m, P::MINW), k));
+    for (int s = 1; s < N; ++s) {
+        const int j = FWD ? s : N - 1 - s;
+        const int jp = FWD ? j - 1 : j + 1;
+        m[j] = P::mx(m[j], P::mn(m[jp], k[j]));
+    }
+    const int first = FWD ? 0 : N - 1, last = FWD ? N - 1 : 0;
     const int edge_lane = FWD ? 0 : 31;
-    const uint32_t out_px = FWD ? P::last(m) : P::first(m);
-    uint32_t in_px = FWD ? __shfl_up_sync(FULL, out_px, 1) : __shfl_down_sync(FULL, out_px, 1);
+    uint32_t in_px = FWD ? __shfl_up_sync(FULL, m[last], 1) : __shfl_down_sync(FULL, m[last], 1);
     if (lane == edge_lane) in_px = cin;
-    const uint32_t k_in = FWD ? P::first(k) : P::last(k);
-    const uint32_t m_in = FWD ? P::first(m) : P::last(m);
     // A carry that does not raise a word's entry pixel raises nothing after it.
-    const bool need = P::gt(P::smin(in_px, k_in), m_in);
-    if (!__any_sync(FULL, need)) return m;
+    const bool need = P::gt(P::mn(in_px, k[first]), m[first]);
+    if (!__any_sync(FULL, need)) return;
 
-    uint32_t A = out_px, B = P::hmin(k);
+    uint32_t A = m[last], B = k[0];
+#pragma unroll
+    for (int j = 1; j < N; ++j) B = P::mn(B, k[j]);
     if (lane == edge_lane) {
-        A = P::smax(A, P::smin(cin, B));
+        A = P::mx(A, P::mn(cin, B));
         B = P::MINPX;  // the entry lane becomes a constant: nothing before it
     }
 #pragma unroll
@@ -217,55 +232,77 @@ __device__ __forceinline__ uint32_t hscan(uint32_t m, uint32_t k, uint32_t cin, 
             Ap = FWD ? __shfl_up_sync(FULL, A, d) : __shfl_down_sync(FULL, A, d);
             Bp = FWD ? __shfl_up_sync(FULL, B, d) : __shfl_down_sync(FULL, B, d);
         } else {
-            uint32_t pk = (A & 0xffffu) | (B << 16);
+            uint32_t pk = A | (B << 16);
             pk = FWD ? __shfl_up_sync(FULL, pk, d) : __shfl_down_sync(FULL, pk, d);
             Ap = pk & 0xffffu;
             Bp = pk >> 16;
         }
         const bool valid = FWD ? (lane >= d) : (lane + d < 32);
         if (valid) {
-            A = P::smax(P::smin(Ap, B), A);
-            B = P::smin(Bp, B);
+            A = P::mx(P::mn(Ap, B), A);
+            B = P::mn(Bp, B);
         }
     }
     uint32_t c = FWD ? __shfl_up_sync(FULL, A, 1) : __shfl_down_sync(FULL, A, 1);
     if (lane == edge_lane) c = cin;
-    return P::vmax(m, P::vmin(P::bcast(c), P::template scanmin<FWD>(k)));
+#pragma unroll
+    for (int s = 0; s < N; ++s) {
+        const int j = FWD ? s : N - 1 - s;
+        c = P::mn(c, k[j]);
+        m[j] = P::mx(m[j], c);
+    }
 }
 
 // ------------------------------------------------------------- one sweep
 // DOWN = raster order (rows top to bottom, each row left to right),
 // otherwise anti-raster.  After a complete raster sweep every pixel satisfies
 // its constraints towards N+ = {left, up-left, up, up-right}; after an
-// anti-raster sweep towards N-.  Returns whether any pixel rose.
+// anti-raster sweep towards N-.  Returns whether any pixel rose; records
+// which rows rose and whether the tile's first / last column rose.
 template <int DT, int CONN, int TH, bool DOWN>
-__device__ __forceinline__ bool sweep(WarpSmem<TH>& sm, uint32_t halo_row, int lane,
-                                      unsigned long long& rows_changed) {
+__device__ __forceinline__ bool sweep(WarpSmem<TH>& sm, int lane, unsigned long long& rows_changed,
+                                      bool& col_changed) {
     using P = Px<DT>;
+    constexpr int N = P::PPW;
     bool any = false;
-    uint32_t prev = halo_row;  // final values of the row processed before
-#pragma unroll 2
+    uint32_t prev[N];
+    P::unpack(sm.tm[(DOWN ? 0 : TH + 1) * 32 + lane], prev);
+#pragma unroll 1
     for (int i = 0; i < TH; ++i) {
-        const int r = DOWN ? i : TH - 1 - i;
-        const int rp = DOWN ? r - 1 : r + 1;  // row of `prev` (-1 / TH = halo)
-        const uint32_t old = sm.tm[r * kRowStride + lane];
-        const uint32_t kr = sm.tk[r * kRowStride + lane];
-        uint32_t v = prev;
+        const int r = DOWN ? 1 + i : TH - i;  // SMEM row
+        const int rp = DOWN ? r - 1 : r + 1;  // SMEM row of `prev`
+        const uint32_t old = sm.tm[r * 32 + lane];
+        uint32_t m[N], k[N];
+        P::unpack(old, m);
+        P::unpack(sm.tk[r * 32 + lane], k);
         if (CONN == 8) {
-            uint32_t pw = __shfl_up_sync(FULL, prev, 1);
-            uint32_t nw = __shfl_down_sync(FULL, prev, 1);
-            if (lane == 0) pw = P::as_last(sm.hLm[rp + 1]);
-            if (lane == 31) nw = sm.hRm[rp + 1];
-            v = P::vmax(v, P::vmax(P::shl1(prev, pw), P::shr1(prev, nw)));
+            uint32_t left = __shfl_up_sync(FULL, prev[N - 1], 1);
+            uint32_t right = __shfl_down_sync(FULL, prev[0], 1);
+            if (lane == 0) left = sm.hLm[rp];
+            if (lane == 31) right = sm.hRm[rp];
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+                const uint32_t a = j == 0 ? left : prev[j - 1];
+                const uint32_t b = j == N - 1 ? right : prev[j + 1];
+                m[j] = P::mx(m[j], P::mn(P::mx3(a, prev[j], b), k[j]));
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < N; ++j) m[j] = P::mx(m[j], P::mn(prev[j], k[j]));
         }
-        uint32_t x = P::vmax(old, P::vmin(v, kr));
-        x = hscan<DT, DOWN>(x, kr, DOWN ? sm.hLm[r + 1] : sm.hRm[r + 1], lane);
-        if (__any_sync(FULL, x != old)) {
-            sm.tm[r * kRowStride + lane] = x;
-            rows_changed |= 1ull << r;
+        hscan<DT, DOWN>(m, k, DOWN ? sm.hLm[r] : sm.hRm[r], lane);
+        const uint32_t nw = P::pack(m);
+        const bool ch = nw != old;
+        if (__any_sync(FULL, ch)) {
+            sm.tm[r * 32 + lane] = nw;
+            rows_changed |= 1ull << (r - 1);
             any = true;
+            uint32_t o[N];
+            P::unpack(old, o);
+            col_changed |= (lane == 0 && m[0] != o[0]) || (lane == 31 && m[N - 1] != o[N - 1]);
         }
-        prev = x;
+#pragma unroll
+        for (int j = 0; j < N; ++j) prev[j] = m[j];
     }
     __syncwarp();
     return any;
@@ -273,44 +310,35 @@ __device__ __forceinline__ bool sweep(WarpSmem<TH>& sm, uint32_t halo_row, int l
 
 // --------------------------------------------------------------- tile visit
 struct VisitResult {
-    unsigned nb;      // NB_* bits: neighbours whose pixels this tile can raise
+    unsigned nb;      // NB_* bits: neighbours to notify
     unsigned sweeps;  // sweeps run
-    bool wrote;       // any pixel of this tile rose
+    bool ok;          // false: a bounded wait ran out (job error)
 };
 
 template <int DT>
-__device__ __forceinline__ void load_word(const unsigned char* mrow, const unsigned char* krow, int npx,
-                                          uint32_t& mw, uint32_t& kw) {
+__device__ __forceinline__ uint32_t load_word_plain(const unsigned char* row, int npx, bool coherent) {
     using P = Px<DT>;
-    if (npx >= P::PPW) {
-        mw = __ldcg(reinterpret_cast<const unsigned int*>(mrow));
-        kw = __ldg(reinterpret_cast<const unsigned int*>(krow));
-    } else if (P::PPW == 1) {
-        mw = P::MINW;
-        kw = P::MINW;
-    } else {
-        // partial word at the right image edge: per-pixel loads, the rest
-        // filled with the type's minimum (inert: it never rises or raises)
-        mw = 0u;
-        kw = 0u;
+    if (npx >= P::PPW)
+        return coherent ? __ldcg(reinterpret_cast<const unsigned int*>(row))
+                        : __ldg(reinterpret_cast<const unsigned int*>(row));
+    uint32_t p[P::PPW];
 #pragma unroll
-        for (int i = 0; i < P::PPW; ++i) {
-            if (i < npx) {
-                mw |= P::ld_px_cg(mrow + i * P::BPP) << (8 * P::BPP * i);
-                kw |= P::ld_px(krow + i * P::BPP) << (8 * P::BPP * i);
-            }
-        }
-    }
+    for (int i = 0; i < P::PPW; ++i)
+        p[i] = i < npx ? (coherent ? P::ld_px_cg(row + i * P::BPP) : P::ld_px(row + i * P::BPP)) : P::MINPX;
+    return P::pack(p);
 }
 
 // One warp: fetch tile (tx, ty) of image d with its one-pixel halo, run
 // raster / anti-raster sweeps until a sweep after the first changes nothing,
-// store the rows that rose, and report every neighbour tile holding a pixel q
-// next to a pixel p of this tile with marker[q] < min(marker[p], mask[q]).
+// store the rows that rose, and report the neighbour tiles to notify: those
+// holding a pixel q next to a pixel p of this tile with
+// marker[q] < min(marker[p], mask[q]) where p's side of the tile rose.
 template <int DT, int CONN, int TH>
-__device__ __noinline__ VisitResult visit_tile(const ImgDesc& d, int tx, int ty, WarpSmem<TH>& sm, int lane) {
+__device__ __noinline__ VisitResult visit_tile(const ImgDesc& d, int tx, int ty, WarpSmem<TH>& sm, int lane,
+                                               unsigned& phase, long long timeout_ns) {
     using P = Px<DT>;
     constexpr int TW = 32 * P::PPW;
+    VisitResult res{0u, 0u, true};
     const int x0 = tx * TW, y0 = ty * TH;
     const int W = d.W, H = d.H;
     const int px0 = x0 + lane * P::PPW;  // first pixel of this lane's word
@@ -318,31 +346,38 @@ __device__ __noinline__ VisitResult visit_tile(const ImgDesc& d, int tx, int ty,
     const size_t col_off = (size_t)(npx > 0 ? px0 : 0) * P::BPP;
     const int rows = min(TH, H - y0);
 
-    // ---- fetch (MR.cu:232-312): interior words, coalesced 128-byte rows
-#pragma unroll 4
-    for (int r = 0; r < TH; ++r) {
-        uint32_t mw = P::MINW, kw = P::MINW;
-        if (r < rows && npx > 0) {
-            const int y = y0 + r;
-            load_word<DT>(d.marker + (size_t)y * d.pitch_m + col_off, d.mask + (size_t)y * d.pitch_k + col_off, npx,
-                          mw, kw);
+    // ---- fetch (MR.cu:232-312)
+    const bool tma = d.tmaps != nullptr;
+    if (tma) {
+        // one box of TH+2 rows x 128 bytes per plane, halo rows included;
+        // rows / columns outside the image arrive as zeros
+        fence_proxy_async_smem();  // earlier generic reads of tm / tk before the async writes
+        __syncwarp();
+        if (lane == 0) {
+            fence_proxy_async_global();
+            mbar_arrive_expect_tx(&sm.mbar, 2u * 128u * (TH + 2));
+            const unsigned char* maps = static_cast<const unsigned char*>(d.tmaps);
+            tma_load_2d(sm.tm, maps, x0 * P::BPP, y0 - 1, &sm.mbar);
+            tma_load_2d(sm.tk, maps + 128, x0 * P::BPP, y0 - 1, &sm.mbar);
         }
-        sm.tm[r * kRowStride + lane] = mw;
-        sm.tk[r * kRowStride + lane] = kw;
+    } else {
+#pragma unroll 8
+        for (int r = 0; r < TH + 2; ++r) {
+            const int y = y0 - 1 + r;
+            uint32_t mw = P::MINW, kw = P::MINW;
+            if (y >= 0 && y < H && npx > 0) {
+                mw = load_word_plain<DT>(d.marker + (size_t)y * d.pitch_m + col_off, npx, true);
+                kw = load_word_plain<DT>(d.mask + (size_t)y * d.pitch_k + col_off, npx, false);
+            }
+            sm.tm[r * 32 + lane] = mw;
+            sm.tk[r * 32 + lane] = kw;
+        }
     }
-    uint32_t top_m = P::MINW, top_k = P::MINW, bot_m = P::MINW, bot_k = P::MINW;
-    if (npx > 0) {
-        if (y0 > 0)
-            load_word<DT>(d.marker + (size_t)(y0 - 1) * d.pitch_m + col_off,
-                          d.mask + (size_t)(y0 - 1) * d.pitch_k + col_off, npx, top_m, top_k);
-        if (y0 + TH < H)
-            load_word<DT>(d.marker + (size_t)(y0 + TH) * d.pitch_m + col_off,
-                          d.mask + (size_t)(y0 + TH) * d.pitch_k + col_off, npx, bot_m, bot_k);
-    }
+    // halo columns (single pixels), in flight together with the box loads
     for (int i = lane; i < TH + 2; i += 32) {
-        const int y = y0 + i - 1;
+        const int y = y0 - 1 + i;
         uint32_t lm = P::MINPX, lk = P::MINPX, rm = P::MINPX, rk = P::MINPX;
-        if (y >= 0 && y < H && i - 1 < rows + 1) {
+        if (y >= 0 && y < H) {
             const unsigned char* mrow = d.marker + (size_t)y * d.pitch_m;
             const unsigned char* krow = d.mask + (size_t)y * d.pitch_k;
             if (x0 > 0) {
@@ -359,90 +394,136 @@ __device__ __noinline__ VisitResult visit_tile(const ImgDesc& d, int tx, int ty,
         sm.hRm[i] = rm;
         sm.hRk[i] = rk;
     }
+    if (tma) {
+        // bounded wait for the box loads
+        const long long t0 = globaltimer_ns();
+        unsigned spins = 0;
+        while (!mbar_try_wait(&sm.mbar, phase)) {
+            if ((++spins & 1023u) == 0u && globaltimer_ns() - t0 > timeout_ns) {
+                res.ok = false;
+                break;
+            }
+        }
+        phase ^= 1u;
+        if (!res.ok) return res;
+        if (DT == DT_I32) {
+            // zero fill is not the int32 minimum: rewrite what lies outside
+            if (y0 == 0) sm.tm[lane] = sm.tk[lane] = P::MINW;
+            for (int r = rows + 1; r < TH + 2; ++r) {
+                if (y0 - 1 + r >= H) sm.tm[r * 32 + lane] = sm.tk[r * 32 + lane] = P::MINW;
+            }
+            if (npx <= 0)
+                for (int r = 0; r < TH + 2; ++r) sm.tm[r * 32 + lane] = sm.tk[r * 32 + lane] = P::MINW;
+        }
+    }
     __syncwarp();
 
     // ---- local convergence (MR.cu:320-325, here with full-length scans)
     unsigned long long rows_changed = 0ull;
+    bool col_changed = false;
     unsigned sweeps = 0;
     for (;;) {
-        const bool ch = (sweeps & 1u) == 0u ? sweep<DT, CONN, TH, true>(sm, top_m, lane, rows_changed)
-                                            : sweep<DT, CONN, TH, false>(sm, bot_m, lane, rows_changed);
+        const bool ch = (sweeps & 1u) == 0u ? sweep<DT, CONN, TH, true>(sm, lane, rows_changed, col_changed)
+                                            : sweep<DT, CONN, TH, false>(sm, lane, rows_changed, col_changed);
         ++sweeps;
         if (!ch && sweeps >= 2) break;
     }
+    res.sweeps = sweeps;
+    if (rows_changed == 0ull) return res;  // nothing rose: nothing to store or notify
 
     // ---- write back the rows that rose (own tile only; MR.cu:335-364)
-    if (rows_changed != 0ull && npx > 0) {
+    if (npx > 0) {
         for (int r = 0; r < rows; ++r) {
             if ((rows_changed >> r) & 1ull) {
                 unsigned char* mrow = d.marker + (size_t)(y0 + r) * d.pitch_m + col_off;
-                const uint32_t w = sm.tm[r * kRowStride + lane];
+                const uint32_t w = sm.tm[(r + 1) * 32 + lane];
                 if (npx >= P::PPW) {
                     __stcg(reinterpret_cast<unsigned int*>(mrow), w);
                 } else {
+                    uint32_t p[P::PPW];
+                    P::unpack(w, p);
 #pragma unroll
                     for (int i = 0; i < P::PPW; ++i)
-                        if (i < npx) P::st_px(mrow + i * P::BPP, P::get(w, i));
+                        if (i < npx) P::st_px(mrow + i * P::BPP, p[i]);
                 }
             }
         }
     }
 
-    // ---- neighbour detection (MR.cu:366-512, pull form): which neighbour
-    // tiles hold a pixel q that some pixel p of this tile can raise.
+    // ---- neighbour detection (MR.cu:366-512, pull form)
+    const bool top_rose = rows_changed & 1ull;
+    const bool bot_rose = (rows_changed >> (TH - 1)) & 1ull;
+    const bool side_rose = __any_sync(FULL, col_changed);
     unsigned nb = 0u;
     {
-        const uint32_t r0 = sm.tm[lane], r1 = sm.tm[(TH - 1) * kRowStride + lane];
-        uint32_t v0 = r0, v1 = r1;
-        if (CONN == 8) {
-            uint32_t pw0 = __shfl_up_sync(FULL, r0, 1), nw0 = __shfl_down_sync(FULL, r0, 1);
-            uint32_t pw1 = __shfl_up_sync(FULL, r1, 1), nw1 = __shfl_down_sync(FULL, r1, 1);
-            if (lane == 0) pw0 = pw1 = P::MINW;
-            if (lane == 31) nw0 = nw1 = P::MINW;
-            v0 = P::vmax(v0, P::vmax(P::shl1(r0, pw0), P::shr1(r0, nw0)));
-            v1 = P::vmax(v1, P::vmax(P::shl1(r1, pw1), P::shr1(r1, nw1)));
-        }
-        if (__any_sync(FULL, P::any_gt(P::vmin(v0, top_k), top_m))) nb |= NB_N;
-        if (__any_sync(FULL, P::any_gt(P::vmin(v1, bot_k), bot_m))) nb |= NB_S;
-
-        // W / E: lanes walk the tile's first / last pixel column (rows lane,
-        // lane+32, ...); stride-33 rows keep these reads conflict-free.
-        bool need_w = false, need_e = false;
-        for (int r = lane; r < TH; r += 32) {
-            uint32_t fv = P::first(sm.tm[r * kRowStride]);
-            uint32_t lv = P::last(sm.tm[r * kRowStride + 31]);
+        uint32_t r0[P::PPW], r1[P::PPW], t_m[P::PPW], t_k[P::PPW], b_m[P::PPW], b_k[P::PPW];
+        P::unpack(sm.tm[32 + lane], r0);
+        P::unpack(sm.tm[TH * 32 + lane], r1);
+        P::unpack(sm.tm[lane], t_m);
+        P::unpack(sm.tk[lane], t_k);
+        P::unpack(sm.tm[(TH + 1) * 32 + lane], b_m);
+        P::unpack(sm.tk[(TH + 1) * 32 + lane], b_k);
+        uint32_t l0 = __shfl_up_sync(FULL, r0[P::PPW - 1], 1), n0 = __shfl_down_sync(FULL, r0[0], 1);
+        uint32_t l1 = __shfl_up_sync(FULL, r1[P::PPW - 1], 1), n1 = __shfl_down_sync(FULL, r1[0], 1);
+        if (lane == 0) l0 = l1 = P::MINPX;  // pixels of other tiles are not sources here
+        if (lane == 31) n0 = n1 = P::MINPX;
+        bool need_n = false, need_s = false;
+#pragma unroll
+        for (int j = 0; j < P::PPW; ++j) {
+            uint32_t v0 = r0[j], v1 = r1[j];
             if (CONN == 8) {
-                if (r > 0) {
-                    fv = P::smax(fv, P::first(sm.tm[(r - 1) * kRowStride]));
-                    lv = P::smax(lv, P::last(sm.tm[(r - 1) * kRowStride + 31]));
-                }
-                if (r + 1 < TH) {
-                    fv = P::smax(fv, P::first(sm.tm[(r + 1) * kRowStride]));
-                    lv = P::smax(lv, P::last(sm.tm[(r + 1) * kRowStride + 31]));
-                }
+                v0 = P::mx3(j == 0 ? l0 : r0[j - 1], v0, j == P::PPW - 1 ? n0 : r0[j + 1]);
+                v1 = P::mx3(j == 0 ? l1 : r1[j - 1], v1, j == P::PPW - 1 ? n1 : r1[j + 1]);
             }
-            need_w |= P::gt(P::smin(fv, sm.hLk[r + 1]), sm.hLm[r + 1]);
-            need_e |= P::gt(P::smin(lv, sm.hRk[r + 1]), sm.hRm[r + 1]);
+            need_n |= P::gt(P::mn(v0, t_k[j]), t_m[j]);
+            need_s |= P::gt(P::mn(v1, b_k[j]), b_m[j]);
         }
-        if (__any_sync(FULL, need_w)) nb |= NB_W;
-        if (__any_sync(FULL, need_e)) nb |= NB_E;
+        if (top_rose && __any_sync(FULL, need_n)) nb |= NB_N;
+        if (bot_rose && __any_sync(FULL, need_s)) nb |= NB_S;
 
+        if (side_rose) {
+            // W / E: lanes walk the tile's first / last pixel column
+            bool need_w = false, need_e = false;
+            for (int r = 1 + lane; r <= TH; r += 32) {
+                uint32_t f[P::PPW], l[P::PPW];
+                P::unpack(sm.tm[r * 32], f);
+                P::unpack(sm.tm[r * 32 + 31], l);
+                uint32_t fv = f[0], lv = l[P::PPW - 1];
+                if (CONN == 8) {
+                    uint32_t fa[P::PPW], la[P::PPW];
+                    if (r > 1) {
+                        P::unpack(sm.tm[(r - 1) * 32], fa);
+                        P::unpack(sm.tm[(r - 1) * 32 + 31], la);
+                        fv = P::mx(fv, fa[0]);
+                        lv = P::mx(lv, la[P::PPW - 1]);
+                    }
+                    if (r < TH) {
+                        P::unpack(sm.tm[(r + 1) * 32], fa);
+                        P::unpack(sm.tm[(r + 1) * 32 + 31], la);
+                        fv = P::mx(fv, fa[0]);
+                        lv = P::mx(lv, la[P::PPW - 1]);
+                    }
+                }
+                need_w |= P::gt(P::mn(fv, sm.hLk[r]), sm.hLm[r]);
+                need_e |= P::gt(P::mn(lv, sm.hRk[r]), sm.hRm[r]);
+            }
+            if (__any_sync(FULL, need_w)) nb |= NB_W;
+            if (__any_sync(FULL, need_e)) nb |= NB_E;
+        }
         if (CONN == 8) {
-            const uint32_t p_nw = P::first(sm.tm[0]);
-            const uint32_t p_ne = P::last(sm.tm[31]);
-            const uint32_t p_sw = P::first(sm.tm[(TH - 1) * kRowStride]);
-            const uint32_t p_se = P::last(sm.tm[(TH - 1) * kRowStride + 31]);
-            if (P::gt(P::smin(p_nw, sm.hLk[0]), sm.hLm[0])) nb |= NB_NW;
-            if (P::gt(P::smin(p_ne, sm.hRk[0]), sm.hRm[0])) nb |= NB_NE;
-            if (P::gt(P::smin(p_sw, sm.hLk[TH + 1]), sm.hLm[TH + 1])) nb |= NB_SW;
-            if (P::gt(P::smin(p_se, sm.hRk[TH + 1]), sm.hRm[TH + 1])) nb |= NB_SE;
+            uint32_t a[P::PPW], b[P::PPW], c[P::PPW], e[P::PPW];
+            P::unpack(sm.tm[32], a);
+            P::unpack(sm.tm[32 + 31], b);
+            P::unpack(sm.tm[TH * 32], c);
+            P::unpack(sm.tm[TH * 32 + 31], e);
+            if (top_rose && P::gt(P::mn(a[0], sm.hLk[0]), sm.hLm[0])) nb |= NB_NW;
+            if (top_rose && P::gt(P::mn(b[P::PPW - 1], sm.hRk[0]), sm.hRm[0])) nb |= NB_NE;
+            if (bot_rose && P::gt(P::mn(c[0], sm.hLk[TH + 1]), sm.hLm[TH + 1])) nb |= NB_SW;
+            if (bot_rose && P::gt(P::mn(e[P::PPW - 1], sm.hRk[TH + 1]), sm.hRm[TH + 1])) nb |= NB_SE;
         }
     }
     __syncwarp();
-    VisitResult res;
     res.nb = nb;
-    res.sweeps = sweeps;
-    res.wrote = rows_changed != 0ull;
     return res;
 }
 

@@ -6,12 +6,6 @@
 
 namespace iwpp {
 
-__device__ __forceinline__ long long globaltimer_ns() {
-    long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
 __device__ __forceinline__ unsigned ld_volatile(const unsigned* p) { return *(const volatile unsigned*)p; }
 __device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
 
@@ -31,15 +25,16 @@ __device__ __forceinline__ int find_image(const EngineArgs& a, unsigned g) {
 }
 
 template <int TH>
-__device__ __forceinline__ VisitResult dispatch_visit(const ImgDesc& d, int tx, int ty, WarpSmem<TH>& sm, int lane) {
+__device__ __forceinline__ VisitResult dispatch_visit(const ImgDesc& d, int tx, int ty, WarpSmem<TH>& sm, int lane,
+                                                     unsigned& phase, long long timeout_ns) {
     const int mode = d.dtype * 2 + (d.conn == 8 ? 1 : 0);
     switch (mode) {
-        case 0: return visit_tile<DT_U8, 4, TH>(d, tx, ty, sm, lane);
-        case 1: return visit_tile<DT_U8, 8, TH>(d, tx, ty, sm, lane);
-        case 2: return visit_tile<DT_U16, 4, TH>(d, tx, ty, sm, lane);
-        case 3: return visit_tile<DT_U16, 8, TH>(d, tx, ty, sm, lane);
-        case 4: return visit_tile<DT_I32, 4, TH>(d, tx, ty, sm, lane);
-        default: return visit_tile<DT_I32, 8, TH>(d, tx, ty, sm, lane);
+        case 0: return visit_tile<DT_U8, 4, TH>(d, tx, ty, sm, lane, phase, timeout_ns);
+        case 1: return visit_tile<DT_U8, 8, TH>(d, tx, ty, sm, lane, phase, timeout_ns);
+        case 2: return visit_tile<DT_U16, 4, TH>(d, tx, ty, sm, lane, phase, timeout_ns);
+        case 3: return visit_tile<DT_U16, 8, TH>(d, tx, ty, sm, lane, phase, timeout_ns);
+        case 4: return visit_tile<DT_I32, 4, TH>(d, tx, ty, sm, lane, phase, timeout_ns);
+        default: return visit_tile<DT_I32, 8, TH>(d, tx, ty, sm, lane, phase, timeout_ns);
     }
 }
 
@@ -71,29 +66,21 @@ __device__ __forceinline__ void mutex_unlock(const EngineArgs& a) {
     atomicExch(&a.ctrl->lock, 0);
 }
 
-// ---------------------------------------------------------------- notify
-// Marks the neighbour tiles in `nb` DIRTY and inserts them into the queue
-// (VAR_UNIQUE: only tiles that were neither pending nor being visited).
-// One lane per direction, one queue reservation per warp.
+// ------------------------------------------------------------------ push
+// Inserts the entries of the lanes with `want` set into the queue: the mutex
+// stack under one lock acquisition (IWPP MP/src/globalQueue.cu:25-81), or the
+// write queue with one atomicAdd reservation per warp
+// (IWPP MP DQ/src/globalQueue.cu:14-47).  A short insertion sets the
+// overflow flag (the reference's memLeak, MR.cu:524-526); the tiles stay
+// DIRTY and are recovered by the restart.
 template <int VAR>
-__device__ void notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty, unsigned nb, int lane, unsigned* wq,
-                       WarpCounters& cnt) {
-    bool want = false;
-    unsigned gn = 0u;
-    if (lane < 8 && ((nb >> lane) & 1u)) {
-        const int nx = tx + kNbDx[lane], ny = ty + kNbDy[lane];
-        if (nx >= 0 && nx < d.tiles_x && ny >= 0 && ny < d.tiles_y) {
-            gn = (unsigned)d.tile_base + (unsigned)(ny * d.tiles_x + nx);
-            const unsigned old = atomicOr(&a.state[gn], ST_DIRTY);
-            want = VAR == VAR_UNIQUE ? (old & (ST_DIRTY | ST_ACTIVE)) == 0u : true;
-        }
-    }
+__device__ void push_entries(const EngineArgs& a, bool want, unsigned gn, int lane, unsigned* wq,
+                             WarpCounters& cnt) {
     const unsigned ballot = __ballot_sync(FULL, want);
     if (ballot == 0u) return;
     const int n = __popc(ballot);
     const int rank = __popc(ballot & ((1u << lane) - 1u));
     if (VAR == VAR_MUTEX) {
-        // IWPP MP/src/globalQueue.cu:25-81: all n entries under one lock
         int base = -1;
         if (lane == 0) {
             if (mutex_lock(a)) {
@@ -102,7 +89,7 @@ __device__ void notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty, un
                     base = top;
                     atomicAdd(&a.ctrl->pending, n);  // before the entries can be taken
                 } else {
-                    atomicExch(&a.ctrl->overflow, 1u);  // MR.cu:524-526 (memLeak)
+                    atomicExch(&a.ctrl->overflow, 1u);
                     mutex_unlock(a);
                 }
             }
@@ -116,9 +103,7 @@ __device__ void notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty, un
             *(volatile int*)&a.ctrl->top = base + n;
             mutex_unlock(a);
         }
-        cnt.pushes += (unsigned)n;
     } else {
-        // IWPP MP DQ/src/globalQueue.cu:14-47, aggregated per warp
         unsigned base = 0u;
         if (lane == 0) base = atomicAdd(&a.ctrl->wn, (unsigned)n);
         base = __shfl_sync(FULL, base, 0);
@@ -129,45 +114,67 @@ __device__ void notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty, un
             else
                 atomicExch(&a.ctrl->overflow, 1u);
         }
-        cnt.pushes += (unsigned)n;
     }
+    cnt.pushes += (unsigned)n;
+}
+
+// Marks the neighbour tiles in `nb` DIRTY and inserts them (VAR_UNIQUE:
+// only those that were neither pending nor being visited).
+template <int VAR>
+__device__ void notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty, unsigned nb, int lane, unsigned* wq,
+                       WarpCounters& cnt) {
+    bool want = false;
+    unsigned gn = 0u;
+    if (lane < 8 && ((nb >> lane) & 1u)) {
+        const int nx = tx + kNbDx[lane], ny = ty + kNbDy[lane];
+        if (nx >= 0 && nx < d.tiles_x && ny >= 0 && ny < d.tiles_y) {
+            gn = (unsigned)d.tile_base + (unsigned)(ny * d.tiles_x + nx);
+            const unsigned old = atomicOr(&a.state[gn], ST_DIRTY);
+            want = VAR == VAR_UNIQUE ? (old & (ST_DIRTY | ST_ACTIVE)) == 0u : true;
+        }
+    }
+    push_entries<VAR>(a, want, gn, lane, wq, cnt);
 }
 
 // ------------------------------------------------------------ one entry
-// Takes tile g (if no other warp owns it) and visits it until it is clean.
+// Takes tile g unless another warp owns it (that owner sees DIRTY when it
+// releases), visits it once if it is DIRTY, notifies the neighbours it
+// raised, and releases it; if it was marked DIRTY meanwhile it is queued
+// again (next round for the double / unique queues) instead of being
+// revisited at once with half-updated neighbours.
 template <int VAR, int TH>
-__device__ void process_entry(const EngineArgs& a, unsigned g, WarpSmem<TH>& sm, int lane, unsigned* wq,
-                              WarpCounters& cnt) {
+__device__ bool process_entry(const EngineArgs& a, unsigned g, WarpSmem<TH>& sm, int lane, unsigned* wq,
+                              WarpCounters& cnt, unsigned& phase) {
     unsigned old = 0u;
     if (lane == 0) old = atomicOr(&a.state[g], ST_ACTIVE);
     old = __shfl_sync(FULL, old, 0);
-    if (old & ST_ACTIVE) return;  // owned elsewhere; DIRTY is set and the owner revisits
-
-    const int ii = find_image(a, g);
-    const ImgDesc d = a.imgs[ii];
-    const int t = (int)(g - (unsigned)d.tile_base);
-    const int ty = t / d.tiles_x, tx = t - ty * d.tiles_x;
-    for (;;) {
-        if (lane == 0) old = atomicAnd(&a.state[g], ~ST_DIRTY);
-        old = __shfl_sync(FULL, old, 0);
-        if ((old & ST_DIRTY) == 0u) {
-            unsigned prev = 0u;
-            if (lane == 0) prev = atomicCAS(&a.state[g], ST_ACTIVE, 0u);
-            prev = __shfl_sync(FULL, prev, 0);
-            if (prev == ST_ACTIVE) return;
-            continue;  // DIRTY came back: visit again
-        }
-        __threadfence();
+    if (old & ST_ACTIVE) return true;
+    if (lane == 0) old = atomicAnd(&a.state[g], ~ST_DIRTY);
+    old = __shfl_sync(FULL, old, 0);
+    if (old & ST_DIRTY) {
+        __threadfence();  // acquire: neighbours' stores before their DIRTY
         __syncwarp();
-        const VisitResult r = dispatch_visit<TH>(d, tx, ty, sm, lane);
+        const int ii = find_image(a, g);
+        const ImgDesc d = a.imgs[ii];
+        const int t = (int)(g - (unsigned)d.tile_base);
+        const int ty = t / d.tiles_x, tx = t - ty * d.tiles_x;
+        const VisitResult r = dispatch_visit<TH>(d, tx, ty, sm, lane, phase, a.timeout_ns);
+        if (!r.ok) {
+            if (lane == 0) set_error(a.ctrl, DEV_ERR_TIMEOUT);
+            return false;
+        }
         cnt.visits += 1;
         cnt.sweeps += r.sweeps;
         if (r.nb != 0u) {
-            __threadfence();  // this tile's stores before the neighbours' DIRTY
+            __threadfence();  // release: this tile's stores before the neighbours' DIRTY
             __syncwarp();
             notify<VAR>(a, d, tx, ty, r.nb, lane, wq, cnt);
         }
     }
+    if (lane == 0) old = atomicAnd(&a.state[g], ~ST_ACTIVE);
+    old = __shfl_sync(FULL, old, 0);
+    if (old & ST_DIRTY) push_entries<VAR>(a, lane == 0, g, lane, wq, cnt);
+    return true;
 }
 
 // ------------------------------------------------------- mutex worker
@@ -178,13 +185,23 @@ __device__ void process_entry(const EngineArgs& a, unsigned g, WarpSmem<TH>& sm,
 // activeBlocksCount (IWPP MP/src/globalQueue.cu:134-145).  On overflow the
 // quiescent stack is refilled with every tile (MR.cu:785-806).
 template <int TH>
-__device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, WarpCounters& cnt) {
+__device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, WarpCounters& cnt, unsigned& phase) {
     long long idle_since = 0;
     unsigned idle_progress = 0u;
     unsigned ns = 64;
     for (;;) {
         int n = 0, base = 0, verdict = 0;  // verdict: 0 work/retry, 1 exit, 2 refill
-        if (lane == 0) {
+        // Test before test-and-set: an idle warp looks at the stack without
+        // the lock and takes it only when there is something to take or the
+        // job looks finished, so idle pollers never starve a warp that
+        // inserts.
+        if (ld_volatile(&a.ctrl->error) != 0u) return;
+        bool try_lock = true;
+        if (lane == 0)
+            try_lock = ld_volatile(&a.ctrl->top) > 0 || ld_volatile(&a.ctrl->pending) == 0 ||
+                       ld_volatile(&a.ctrl->error) != 0u;
+        try_lock = __shfl_sync(FULL, try_lock ? 1 : 0, 0) != 0;
+        if (lane == 0 && try_lock) {
             if (!mutex_lock(a)) {
                 verdict = 1;
             } else {
@@ -255,7 +272,8 @@ __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
         }
         for (int j = 0; j < n; ++j) {
             const unsigned g = __shfl_sync(FULL, mine, j);
-            process_entry<VAR_MUTEX, TH>(a, g, sm, lane, nullptr, cnt);
+            const bool ok = process_entry<VAR_MUTEX, TH>(a, g, sm, lane, nullptr, cnt, phase);
+            if (!ok) return;
             if (lane == 0) {
                 __threadfence();
                 atomicAdd(&a.ctrl->progress, 1u);
@@ -333,7 +351,7 @@ __device__ bool grid_barrier_round(const EngineArgs& a) {
 
 // ------------------------------------------------------- round worker
 template <int VAR, int TH>
-__device__ void round_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, WarpCounters& cnt) {
+__device__ void round_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, WarpCounters& cnt, unsigned& phase) {
     for (;;) {
         const unsigned rn = ld_volatile(&a.ctrl->rn);
         const unsigned vfull = ld_volatile(&a.ctrl->vfull);
@@ -347,7 +365,7 @@ __device__ void round_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
             if (idx >= rn) break;
             if (ld_volatile(&a.ctrl->error) != 0u) break;
             const unsigned g = vfull ? idx : __ldcg(&rq[idx]);
-            process_entry<VAR, TH>(a, g, sm, lane, wq, cnt);
+            if (!process_entry<VAR, TH>(a, g, sm, lane, wq, cnt, phase)) break;
         }
         if (!grid_barrier_round(a)) return;
         if (ld_volatile(&a.ctrl->done) != 0u) return;
@@ -357,14 +375,23 @@ __device__ void round_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
 // --------------------------------------------------------------- kernels
 template <int VAR, int TH>
 __global__ void __launch_bounds__(kWarps * 32) engine_kernel(EngineArgs a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    WarpSmem<TH>& sm = reinterpret_cast<WarpSmem<TH>*>(smem_raw)[warp];
+    // 128-byte align the per-warp areas (the launch adds 128 bytes of slack)
+    const uint32_t base = smem_u32(smem_raw);
+    unsigned char* aligned = smem_raw + ((128u - (base & 127u)) & 127u);
+    WarpSmem<TH>& sm = reinterpret_cast<WarpSmem<TH>*>(aligned)[warp];
+    if (lane == 0) {
+        mbar_init(&sm.mbar, 1u);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    unsigned phase = 0u;
     WarpCounters cnt;
     if (VAR == VAR_MUTEX)
-        mutex_worker<TH>(a, sm, lane, cnt);
+        mutex_worker<TH>(a, sm, lane, cnt, phase);
     else
-        round_worker<VAR, TH>(a, sm, lane, cnt);
+        round_worker<VAR, TH>(a, sm, lane, cnt, phase);
     if (lane == 0) {
         if (cnt.visits) atomicAdd(&a.ctrl->visits, cnt.visits);
         if (cnt.sweeps) atomicAdd(&a.ctrl->sweeps, cnt.sweeps);
@@ -424,7 +451,7 @@ static void* select_kernel(int variant, int tile_rows) {
 }
 
 static size_t smem_bytes(int tile_rows) {
-    return tile_rows == 32 ? kWarps * sizeof(WarpSmem<32>) : kWarps * sizeof(WarpSmem<64>);
+    return 128 + (tile_rows == 32 ? kWarps * sizeof(WarpSmem<32>) : kWarps * sizeof(WarpSmem<64>));
 }
 
 cudaError_t engine_prepare(int variant, int tile_rows, int device, LaunchInfo* li) {

@@ -17,23 +17,10 @@
 namespace iwpp {
 
 template <int DT>
-__device__ __forceinline__ void load_word_plain(const unsigned char* mrow, const unsigned char* krow, int npx,
-                                                uint32_t& mw, uint32_t& kw) {
-    using P = Px<DT>;
-    if (npx >= P::PPW) {
-        mw = *reinterpret_cast<const unsigned int*>(mrow);
-        kw = __ldg(reinterpret_cast<const unsigned int*>(krow));
-    } else {
-        mw = P::PPW == 1 ? P::MINW : 0u;
-        kw = P::PPW == 1 ? P::MINW : 0u;
-#pragma unroll
-        for (int i = 0; i < P::PPW; ++i) {
-            if (i < npx) {
-                mw |= P::ld_px(mrow + i * P::BPP) << (8 * P::BPP * i);
-                kw |= P::ld_px(krow + i * P::BPP) << (8 * P::BPP * i);
-            }
-        }
-    }
+__device__ __forceinline__ void load_pair(const unsigned char* mrow, const unsigned char* krow, int npx,
+                                          uint32_t& mw, uint32_t& kw) {
+    mw = load_word_plain<DT>(mrow, npx, true);
+    kw = load_word_plain<DT>(krow, npx, false);
 }
 
 template <int DT>
@@ -42,9 +29,11 @@ __device__ __forceinline__ void store_word_plain(unsigned char* mrow, int npx, u
     if (npx >= P::PPW) {
         *reinterpret_cast<unsigned int*>(mrow) = w;
     } else {
+        uint32_t p[P::PPW];
+        P::unpack(w, p);
 #pragma unroll
         for (int i = 0; i < P::PPW; ++i)
-            if (i < npx) P::st_px(mrow + i * P::BPP, P::get(w, i));
+            if (i < npx) P::st_px(mrow + i * P::BPP, p[i]);
     }
 }
 
@@ -61,8 +50,13 @@ __global__ void clip_kernel(ImgDesc d) {
         unsigned char* mrow = d.marker + (size_t)y * d.pitch_m + (size_t)px0 * P::BPP;
         const unsigned char* krow = d.mask + (size_t)y * d.pitch_k + (size_t)px0 * P::BPP;
         uint32_t mw, kw;
-        load_word_plain<DT>(mrow, krow, npx, mw, kw);
-        const uint32_t c = P::vmin(mw, kw);
+        load_pair<DT>(mrow, krow, npx, mw, kw);
+        uint32_t m[P::PPW], k[P::PPW];
+        P::unpack(mw, m);
+        P::unpack(kw, k);
+#pragma unroll
+        for (int j = 0; j < P::PPW; ++j) m[j] = P::mn(m[j], k[j]);
+        const uint32_t c = P::pack(m);
         if (c != mw) store_word_plain<DT>(mrow, npx, c);
     }
 }
@@ -83,10 +77,14 @@ __global__ void sweep_x_kernel(ImgDesc d) {
         const int c = FWD ? cc : chunks - 1 - cc;
         const int px0 = c * TW + lane * P::PPW, npx = d.W - px0;
         uint32_t mw = P::MINW, kw = P::MINW;
-        if (npx > 0) load_word_plain<DT>(mbase + (size_t)px0 * P::BPP, kbase + (size_t)px0 * P::BPP, npx, mw, kw);
-        const uint32_t nw = hscan<DT, FWD>(mw, kw, carry, lane);
+        if (npx > 0) load_pair<DT>(mbase + (size_t)px0 * P::BPP, kbase + (size_t)px0 * P::BPP, npx, mw, kw);
+        uint32_t m[P::PPW], k[P::PPW];
+        P::unpack(mw, m);
+        P::unpack(kw, k);
+        hscan<DT, FWD>(m, k, carry, lane);
+        const uint32_t nw = P::pack(m);
         if (npx > 0 && nw != mw) store_word_plain<DT>(mbase + (size_t)px0 * P::BPP, npx, nw);
-        carry = FWD ? __shfl_sync(FULL, P::last(nw), 31) : __shfl_sync(FULL, P::first(nw), 0);
+        carry = FWD ? __shfl_sync(FULL, m[P::PPW - 1], 31) : __shfl_sync(FULL, m[0], 0);
     }
 }
 
@@ -95,28 +93,42 @@ template <int DT, int CONN, bool DOWN>
 __global__ void sweep_y_kernel(ImgDesc d) {
     using P = Px<DT>;
     constexpr int TW = 32 * P::PPW;
+    constexpr int N = P::PPW;
     const int lane = threadIdx.x & 31;
     const int strip = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int strips = (d.W + TW - 1) / TW;
     if (strip >= strips) return;
     const int px0 = strip * TW + lane * P::PPW, npx = d.W - px0;
     const size_t off = (size_t)(npx > 0 ? px0 : 0) * P::BPP;
-    uint32_t prev = P::MINW;
+    uint32_t prev[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) prev[j] = P::MINPX;
     for (int i = 0; i < d.H; ++i) {
         const int y = DOWN ? i : d.H - 1 - i;
         uint32_t mw = P::MINW, kw = P::MINW;
         unsigned char* mrow = d.marker + (size_t)y * d.pitch_m + off;
-        if (npx > 0) load_word_plain<DT>(mrow, d.mask + (size_t)y * d.pitch_k + off, npx, mw, kw);
-        uint32_t v = prev;
+        if (npx > 0) load_pair<DT>(mrow, d.mask + (size_t)y * d.pitch_k + off, npx, mw, kw);
+        uint32_t m[N], k[N];
+        P::unpack(mw, m);
+        P::unpack(kw, k);
         if (CONN == 8) {
-            uint32_t pw = __shfl_up_sync(FULL, prev, 1), nw = __shfl_down_sync(FULL, prev, 1);
-            if (lane == 0) pw = P::MINW;
-            if (lane == 31) nw = P::MINW;
-            v = P::vmax(v, P::vmax(P::shl1(prev, pw), P::shr1(prev, nw)));
+            uint32_t left = __shfl_up_sync(FULL, prev[N - 1], 1), right = __shfl_down_sync(FULL, prev[0], 1);
+            if (lane == 0) left = P::MINPX;
+            if (lane == 31) right = P::MINPX;
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+                const uint32_t a = j == 0 ? left : prev[j - 1];
+                const uint32_t b = j == N - 1 ? right : prev[j + 1];
+                m[j] = P::mx(m[j], P::mn(P::mx3(a, prev[j], b), k[j]));
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < N; ++j) m[j] = P::mx(m[j], P::mn(prev[j], k[j]));
         }
-        const uint32_t x = P::vmax(mw, P::vmin(v, kw));
+        const uint32_t x = P::pack(m);
         if (npx > 0 && x != mw) store_word_plain<DT>(mrow, npx, x);
-        prev = x;
+#pragma unroll
+        for (int j = 0; j < N; ++j) prev[j] = m[j];
     }
 }
 

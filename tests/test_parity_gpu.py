@@ -85,6 +85,18 @@ def test_random_shapes(dt, conn, variant):
         assert np.array_equal(out, ref), (h, w, int((out != ref).sum()))
 
 
+@pytest.mark.parametrize("plain", [0, 1])
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_tma_and_plain_load_paths_agree(plain, variant):
+    # 16-byte aligned images take the TMA box path unless plain loads are forced
+    for dt in (0, 1, 2):
+        mask = synth.noise_mask(1000, 333, dt, 60 + dt, 3.0, 10)
+        marker = synth.hdome_marker(mask, 35)
+        ref = oracle.reconstruct(marker, mask, 8)
+        out, _ = gpu_reconstruct(marker, mask, 8, variant, iwpp.Config.make(plain_loads=plain))
+        assert np.array_equal(out, ref), dt
+
+
 @pytest.mark.parametrize("tile_rows", [32, 64])
 def test_tile_rows_and_noise_without_precondition(tile_rows):
     # raw noise, marker above the mask at half of the pixels
