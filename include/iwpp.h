@@ -40,10 +40,12 @@ typedef enum iwpp_dtype { IWPP_U8 = 0, IWPP_U16 = 1, IWPP_I32 = 2 } iwpp_dtype;
 /* The reference's three global-queue implementations (one per source
  * directory).  Same result, different work queue. */
 typedef enum iwpp_queue_variant {
-    IWPP_QUEUE_DEFAULT = -1, /* IWPP_QUEUE_VARIANT env var, else UNIQUE */
+    IWPP_QUEUE_DEFAULT = -1, /* IWPP_QUEUE_VARIANT env var, else ASYNC */
     IWPP_QUEUE_MUTEX = 0,    /* IWPP MP: LIFO stack under one spin mutex, one persistent launch */
     IWPP_QUEUE_DOUBLE = 1,   /* IWPP MP DQ: read/write queues swapped every round */
-    IWPP_QUEUE_UNIQUE = 2    /* IWPP MP UQ: double queue, each tile at most once per round */
+    IWPP_QUEUE_UNIQUE = 2,   /* IWPP MP UQ: double queue, each tile at most once per round */
+    IWPP_QUEUE_ASYNC = 3     /* no reference counterpart: the unique queue without rounds
+                                (lock-free ring, fetch-and-add claims) */
 } iwpp_queue_variant;
 
 typedef struct iwpp_config {
@@ -144,7 +146,7 @@ IWPP_API int iwpp_sweep_timing(void *marker, const void *mask, size_t pitch_mark
 /* Exactly the reference signature (IWPP MP/include/MorphologicalReconstruction.cuh:45-46;
  * DQ :53-54, UQ :59-60): uint8, square size x size, 4-connectivity, default
  * stream, synchronous, in place on marker.  The queue variant is
- * IWPP_QUEUE_VARIANT (mutex | double | unique), default unique.  Errors are
+ * IWPP_QUEUE_VARIANT (mutex | double | unique | async), default async.  Errors are
  * kept for iwpp_last_status(). */
 IWPP_API void MorphologicalReconstruction(unsigned char *marker, unsigned char *mask, size_t pitchMarker,
                                           size_t pitchMask, int size);

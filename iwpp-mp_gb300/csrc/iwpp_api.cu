@@ -37,15 +37,18 @@ int default_tile_rows(int dtype) {
 }
 
 int resolve_variant(int variant) {
-    if (variant == IWPP_QUEUE_MUTEX || variant == IWPP_QUEUE_DOUBLE || variant == IWPP_QUEUE_UNIQUE) return variant;
+    if (variant == IWPP_QUEUE_MUTEX || variant == IWPP_QUEUE_DOUBLE || variant == IWPP_QUEUE_UNIQUE ||
+        variant == IWPP_QUEUE_ASYNC)
+        return variant;
     const char* e = std::getenv("IWPP_QUEUE_VARIANT");
     if (e) {
         std::string s(e);
         if (s == "mutex" || s == "mp" || s == "MP") return IWPP_QUEUE_MUTEX;
         if (s == "double" || s == "dq" || s == "DQ") return IWPP_QUEUE_DOUBLE;
         if (s == "unique" || s == "uq" || s == "UQ") return IWPP_QUEUE_UNIQUE;
+        if (s == "async") return IWPP_QUEUE_ASYNC;
     }
-    return IWPP_QUEUE_UNIQUE;
+    return IWPP_QUEUE_ASYNC;
 }
 
 struct Config {
@@ -163,7 +166,9 @@ Layout layout_for(long long n_imgs, long long G, long long cap, bool two_queues)
 
 long long queue_capacity_for(int variant, long long G, long long requested) {
     long long cap;
-    if (variant == IWPP_QUEUE_UNIQUE) {
+    if (variant == IWPP_QUEUE_ASYNC) {
+        cap = std::max<long long>(2 * G, 1024);  // ring: at most G entries outstanding
+    } else if (variant == IWPP_QUEUE_UNIQUE) {
         cap = std::max<long long>(G, 1);  // one entry per tile at most
     } else if (requested > 0) {
         cap = variant == IWPP_QUEUE_MUTEX ? std::max(requested, G) : requested;
@@ -347,7 +352,7 @@ int check_device(int device) {
 // Enqueues a prepared job on `s` into workspace `ws`.
 int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool use_events, cudaEvent_t ev0,
                 cudaEvent_t ev1, bool upload_descs) {
-    const bool two = job.variant != IWPP_QUEUE_MUTEX;
+    const bool two = job.variant == IWPP_QUEUE_DOUBLE || job.variant == IWPP_QUEUE_UNIQUE;
     const long long cap = queue_capacity_for(job.variant, job.G, job.cfg.queue_capacity);
     const Layout l = layout_for((long long)job.descs.size(), job.G, cap, two);
     int rc = ensure_workspace(ws, l.total);
@@ -562,7 +567,7 @@ int iwpp_handle_destroy(iwpp_handle h) {
 long long iwpp_workspace_bytes(long long tiles, int variant, long long queue_capacity) {
     const int v = resolve_variant(variant);
     const long long cap = queue_capacity_for(v, tiles, queue_capacity);
-    return (long long)layout_for(1, tiles, cap, v != IWPP_QUEUE_MUTEX).total;
+    return (long long)layout_for(1, tiles, cap, v == IWPP_QUEUE_DOUBLE || v == IWPP_QUEUE_UNIQUE).total;
 }
 
 long long iwpp_tile_count(int width, int height, int dtype, int tile_rows) {
@@ -659,7 +664,7 @@ int iwpp_plan_create(iwpp_plan* out, iwpp_handle h, const iwpp_image* images, in
     }
     if (rc == IWPP_OK) {
         // Workspace and descriptors first (outside the graph, once).
-        const bool two = job.variant != IWPP_QUEUE_MUTEX;
+        const bool two = job.variant == IWPP_QUEUE_DOUBLE || job.variant == IWPP_QUEUE_UNIQUE;
         const long long cap = queue_capacity_for(job.variant, job.G, job.cfg.queue_capacity);
         const Layout l = layout_for((long long)job.descs.size(), job.G, cap, two);
         rc = ensure_workspace(p->ws, l.total);

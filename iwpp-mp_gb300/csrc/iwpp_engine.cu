@@ -103,6 +103,28 @@ __device__ void push_entries(const EngineArgs& a, bool want, unsigned gn, int la
             *(volatile int*)&a.ctrl->top = base + n;
             mutex_unlock(a);
         }
+    } else if (VAR == VAR_ASYNC) {
+        // positions [base, base + n) of the ring; `pending` first, so the job
+        // cannot look finished while these entries exist
+        unsigned base = 0u;
+        if (lane == 0) {
+            atomicAdd(&a.ctrl->pending, n);
+            base = atomicAdd(&a.ctrl->atail, (unsigned)n);
+        }
+        base = __shfl_sync(FULL, base, 0);
+        if (want) {
+            const unsigned slot = (base + (unsigned)rank - a.G) % a.cap;
+            const long long t0 = globaltimer_ns();
+            unsigned spins = 0;
+            // the slot's previous occupant has normally been taken long ago
+            while (atomicCAS(&a.q0[slot], 0u, gn + 1u) != 0u) {
+                __nanosleep(64);
+                if ((++spins & 255u) == 0u && globaltimer_ns() - t0 > a.timeout_ns) {
+                    set_error(a.ctrl, DEV_ERR_TIMEOUT);
+                    break;
+                }
+            }
+        }
     } else {
         unsigned base = 0u;
         if (lane == 0) base = atomicAdd(&a.ctrl->wn, (unsigned)n);
@@ -130,7 +152,7 @@ __device__ void notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty, un
         if (nx >= 0 && nx < d.tiles_x && ny >= 0 && ny < d.tiles_y) {
             gn = (unsigned)d.tile_base + (unsigned)(ny * d.tiles_x + nx);
             const unsigned old = atomicOr(&a.state[gn], ST_DIRTY);
-            want = VAR == VAR_UNIQUE ? (old & (ST_DIRTY | ST_ACTIVE)) == 0u : true;
+            want = (VAR == VAR_UNIQUE || VAR == VAR_ASYNC) ? (old & (ST_DIRTY | ST_ACTIVE)) == 0u : true;
         }
     }
     push_entries<VAR>(a, want, gn, lane, wq, cnt);
@@ -283,6 +305,62 @@ __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
     }
 }
 
+// ------------------------------------------------------- async worker
+// Ring positions 0..G-1 are the initial tiles (no storage); position p >= G
+// lives in slot (p - G) % cap.  A warp claims the next position with one
+// atomicAdd and waits for a producer to fill it.  Every filled position is
+// claimed by exactly one warp, and when `pending` (filled, unfinished
+// entries) reaches zero no producer is left, so waiting warps leave.
+template <int TH>
+__device__ void async_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, WarpCounters& cnt, unsigned& phase) {
+    for (;;) {
+        unsigned p = 0u;
+        if (lane == 0) p = atomicAdd(&a.ctrl->ahead, 1u);
+        p = __shfl_sync(FULL, p, 0);
+        unsigned g = p;
+        if (p >= a.G) {
+            int verdict = 0;  // 0 got an entry, 1 exit
+            unsigned v = 0u;
+            if (lane == 0) {
+                const unsigned slot = (p - a.G) % a.cap;
+                long long idle_since = globaltimer_ns();
+                unsigned idle_progress = ld_volatile(&a.ctrl->progress);
+                unsigned ns = 32;
+                for (;;) {
+                    v = atomicExch(&a.q0[slot], 0u);
+                    if (v != 0u) break;
+                    if (ld_volatile(&a.ctrl->pending) == 0 || ld_volatile(&a.ctrl->error) != 0u) {
+                        verdict = 1;
+                        break;
+                    }
+                    __nanosleep(ns);
+                    if (ns < 2048) ns <<= 1;
+                    const unsigned prog = ld_volatile(&a.ctrl->progress);
+                    const long long now = globaltimer_ns();
+                    if (prog != idle_progress) {
+                        idle_progress = prog;
+                        idle_since = now;
+                    } else if (now - idle_since > a.timeout_ns) {
+                        set_error(a.ctrl, DEV_ERR_TIMEOUT);
+                        verdict = 1;
+                        break;
+                    }
+                }
+            }
+            verdict = __shfl_sync(FULL, verdict, 0);
+            if (verdict) return;
+            g = __shfl_sync(FULL, v, 0) - 1u;
+        }
+        const bool ok = process_entry<VAR_ASYNC, TH>(a, g, sm, lane, nullptr, cnt, phase);
+        if (lane == 0) {
+            __threadfence();
+            atomicAdd(&a.ctrl->progress, 1u);
+            atomicSub(&a.ctrl->pending, 1);  // after this entry's insertions
+        }
+        if (!ok) return;
+    }
+}
+
 // --------------------------------------------------------- grid barrier
 // All CTAs of the (cooperative) launch.  The last CTA to arrive performs the
 // round transition.  Waits are bounded; returns false when the job failed.
@@ -390,6 +468,8 @@ __global__ void __launch_bounds__(kWarps * 32) engine_kernel(EngineArgs a) {
     WarpCounters cnt;
     if (VAR == VAR_MUTEX)
         mutex_worker<TH>(a, sm, lane, cnt, phase);
+    else if (VAR == VAR_ASYNC)
+        async_worker<TH>(a, sm, lane, cnt, phase);
     else
         round_worker<VAR, TH>(a, sm, lane, cnt, phase);
     if (lane == 0) {
@@ -409,6 +489,8 @@ __global__ void engine_init_kernel(EngineArgs a, int variant) {
         a.state[g] = ST_DIRTY;
         if (variant == VAR_MUTEX && g < a.cap) a.q0[g] = a.G - 1u - g;
     }
+    if (variant == VAR_ASYNC)
+        for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < a.cap; i += stride) a.q0[i] = 0u;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         Ctrl* c = a.ctrl;
         c->rn = a.G;
@@ -427,6 +509,9 @@ __global__ void engine_init_kernel(EngineArgs a, int variant) {
         c->top = (int)(a.G < a.cap ? a.G : a.cap);
         c->pending = (int)(a.G < a.cap ? a.G : a.cap);
         c->progress = 0u;
+        c->ahead = 0u;
+        c->atail = a.G;
+        if (variant == VAR_ASYNC) c->pending = (int)a.G;
         c->visits = 0ull;
         c->sweeps = 0ull;
         c->pushes = 0ull;
@@ -443,10 +528,12 @@ static void* select_kernel(int variant, int tile_rows) {
     if (tile_rows == 32) {
         if (variant == VAR_MUTEX) return kernel_ptr<VAR_MUTEX, 32>();
         if (variant == VAR_DOUBLE) return kernel_ptr<VAR_DOUBLE, 32>();
+        if (variant == VAR_ASYNC) return kernel_ptr<VAR_ASYNC, 32>();
         return kernel_ptr<VAR_UNIQUE, 32>();
     }
     if (variant == VAR_MUTEX) return kernel_ptr<VAR_MUTEX, 64>();
     if (variant == VAR_DOUBLE) return kernel_ptr<VAR_DOUBLE, 64>();
+    if (variant == VAR_ASYNC) return kernel_ptr<VAR_ASYNC, 64>();
     return kernel_ptr<VAR_UNIQUE, 64>();
 }
 

@@ -10,8 +10,10 @@
 //          host reads the queue size back every round).
 //   UNIQUE IWPP MP UQ/src/MorphologicalReconstruction.cu:1152-1293
 //          (per-tile flag de-duplication between rounds).
+//   ASYNC  no reference counterpart: the unique queue without rounds, as a
+//          lock-free ring of tile ids claimed and filled with fetch-and-add.
 //
-// GB300 form: one persistent launch for all three.  The double / unique
+// GB300 form: one persistent launch for all of them.  The double / unique
 // rounds are separated by a device-wide barrier (cooperative launch) instead
 // of a host round trip, the unique queue de-duplicates when a tile is
 // inserted, and all insertions are warp-aggregated (one atomic per warp).
@@ -30,7 +32,7 @@
 namespace iwpp {
 
 enum : unsigned { ST_DIRTY = 1u, ST_ACTIVE = 2u };
-enum : int { VAR_MUTEX = 0, VAR_DOUBLE = 1, VAR_UNIQUE = 2 };
+enum : int { VAR_MUTEX = 0, VAR_DOUBLE = 1, VAR_UNIQUE = 2, VAR_ASYNC = 3 };
 enum : unsigned { DEV_OK = 0u, DEV_ERR_TIMEOUT = 3u, DEV_ERR_OVERFLOW = 5u };
 
 constexpr int kWarps = 4;       // warps (independent tile workers) per CTA
@@ -53,6 +55,8 @@ struct Ctrl {
     int top;
     int pending;        // mutex: entries in the stack or taken and unfinished
     unsigned progress;  // finished entries (for the no-progress timeout)
+    unsigned ahead;     // async ring: next position to claim
+    unsigned atail;     // async ring: next position to fill
     unsigned long long visits;
     unsigned long long sweeps;
     unsigned long long pushes;

@@ -23,9 +23,9 @@ from typing import Optional, Sequence
 from . import _build
 
 U8, U16, I32 = 0, 1, 2
-MUTEX, DOUBLE, UNIQUE, DEFAULT = 0, 1, 2, -1
+MUTEX, DOUBLE, UNIQUE, ASYNC, DEFAULT = 0, 1, 2, 3, -1
 VARIANTS = {"mutex": MUTEX, "mp": MUTEX, "double": DOUBLE, "dq": DOUBLE, "unique": UNIQUE, "uq": UNIQUE,
-            "default": DEFAULT}
+            "async": ASYNC, "default": DEFAULT}
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "timeout", 4: "CUDA error",
           5: "queue overflow restarts exhausted", 6: "no sm_103 device", 7: "busy"}

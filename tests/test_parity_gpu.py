@@ -12,7 +12,7 @@ from iwpp import synth
 
 pytestmark = pytest.mark.gpu
 
-VARIANTS = ["mutex", "double", "unique"]
+VARIANTS = ["mutex", "double", "unique", "async"]
 NP = {0: np.uint8, 1: np.uint16, 2: np.int32}
 
 
@@ -175,7 +175,7 @@ def test_reference_compatible_entry_point(monkeypatch):
     mask = synth.noise_mask(size, size, 0, 11, 4.0, 20)
     marker = synth.hdome_marker(mask, 30)
     ref = oracle.reconstruct(marker, mask, 4)
-    for env in ("mutex", "double", "unique"):
+    for env in ("mutex", "double", "unique", "async"):
         monkeypatch.setenv("IWPP_QUEUE_VARIANT", env)
         pitch = 1024  # like cudaMallocPitch
         bm = torch.zeros((size, pitch), dtype=torch.uint8, device="cuda")
