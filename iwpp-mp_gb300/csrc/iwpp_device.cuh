@@ -40,6 +40,7 @@ struct Px<DT_U8> {
     static constexpr int BPP = 1;
     static constexpr uint32_t MINPX = 0u;
     static constexpr uint32_t MINW = 0u;
+    static constexpr uint32_t FIRST_MASK = 0x000000ffu, LAST_MASK = 0xff000000u;
     __device__ static __forceinline__ uint32_t mx(uint32_t a, uint32_t b) { return max(a, b); }
     __device__ static __forceinline__ uint32_t mn(uint32_t a, uint32_t b) { return min(a, b); }
     __device__ static __forceinline__ uint32_t mx3(uint32_t a, uint32_t b, uint32_t c) { return __vimax3_u32(a, b, c); }
@@ -66,6 +67,7 @@ struct Px<DT_U16> {
     static constexpr int BPP = 2;
     static constexpr uint32_t MINPX = 0u;
     static constexpr uint32_t MINW = 0u;
+    static constexpr uint32_t FIRST_MASK = 0x0000ffffu, LAST_MASK = 0xffff0000u;
     __device__ static __forceinline__ uint32_t mx(uint32_t a, uint32_t b) { return max(a, b); }
     __device__ static __forceinline__ uint32_t mn(uint32_t a, uint32_t b) { return min(a, b); }
     __device__ static __forceinline__ uint32_t mx3(uint32_t a, uint32_t b, uint32_t c) { return __vimax3_u32(a, b, c); }
@@ -92,6 +94,7 @@ struct Px<DT_I32> {
     static constexpr int BPP = 4;
     static constexpr uint32_t MINPX = 0x80000000u;
     static constexpr uint32_t MINW = 0x80000000u;
+    static constexpr uint32_t FIRST_MASK = 0xffffffffu, LAST_MASK = 0xffffffffu;
     __device__ static __forceinline__ uint32_t mx(uint32_t a, uint32_t b) { return (uint32_t)max((int)a, (int)b); }
     __device__ static __forceinline__ uint32_t mn(uint32_t a, uint32_t b) { return (uint32_t)min((int)a, (int)b); }
     __device__ static __forceinline__ uint32_t mx3(uint32_t a, uint32_t b, uint32_t c) {
@@ -257,20 +260,30 @@ __device__ __forceinline__ void hscan(uint32_t (&m)[Px<DT>::PPW], const uint32_t
 // DOWN = raster order (rows top to bottom, each row left to right),
 // otherwise anti-raster.  After a complete raster sweep every pixel satisfies
 // its constraints towards N+ = {left, up-left, up, up-right}; after an
-// anti-raster sweep towards N-.  Returns whether any pixel rose; records
-// which rows rose and whether the tile's first / last column rose.
+// anti-raster sweep towards N-.
+//
+// Rows are skipped when nothing they depend on can have changed since they
+// last satisfied this sweep's constraints: a row is processed when the row
+// before it (in sweep order) rose in this sweep, or when it or a vertical
+// neighbour rose in the previous sweep (`dil`, already dilated by one row),
+// or when its halo inputs are new (`force`, folded into `dil` by the caller).
+// `chg` receives the rows that rose (bit r-1 for SMEM row r).
 template <int DT, int CONN, int TH, bool DOWN>
-__device__ __forceinline__ bool sweep(WarpSmem<TH>& sm, int lane, unsigned long long& rows_changed,
-                                      bool& col_changed) {
+__device__ __forceinline__ void sweep(WarpSmem<TH>& sm, int lane, unsigned long long dil, unsigned long long& chg,
+                                      bool& col_changed, uint32_t edge_mask) {
     using P = Px<DT>;
     constexpr int N = P::PPW;
-    bool any = false;
     uint32_t prev[N];
-    P::unpack(sm.tm[(DOWN ? 0 : TH + 1) * 32 + lane], prev);
+    bool prev_valid = false, prev_changed = false;
 #pragma unroll 1
     for (int i = 0; i < TH; ++i) {
         const int r = DOWN ? 1 + i : TH - i;  // SMEM row
-        const int rp = DOWN ? r - 1 : r + 1;  // SMEM row of `prev`
+        const int rp = DOWN ? r - 1 : r + 1;  // SMEM row before it in sweep order
+        if (!prev_changed && !((dil >> (r - 1)) & 1ull)) {
+            prev_valid = false;
+            continue;
+        }
+        if (!prev_valid) P::unpack(sm.tm[rp * 32 + lane], prev);
         const uint32_t old = sm.tm[r * 32 + lane];
         uint32_t m[N], k[N];
         P::unpack(old, m);
@@ -280,11 +293,19 @@ __device__ __forceinline__ bool sweep(WarpSmem<TH>& sm, int lane, unsigned long 
             uint32_t right = __shfl_down_sync(FULL, prev[0], 1);
             if (lane == 0) left = sm.hLm[rp];
             if (lane == 31) right = sm.hRm[rp];
+            if (N == 1) {
+                m[0] = P::mx(m[0], P::mn(P::mx3(left, prev[0], right), k[0]));
+            } else {
+                // shared pairwise maxima of the previous row
+                uint32_t pair[N > 1 ? N - 1 : 1];
 #pragma unroll
-            for (int j = 0; j < N; ++j) {
-                const uint32_t a = j == 0 ? left : prev[j - 1];
-                const uint32_t b = j == N - 1 ? right : prev[j + 1];
-                m[j] = P::mx(m[j], P::mn(P::mx3(a, prev[j], b), k[j]));
+                for (int j = 0; j + 1 < N; ++j) pair[j] = P::mx(prev[j], prev[j + 1]);
+#pragma unroll
+                for (int j = 0; j < N; ++j) {
+                    const uint32_t v = j == 0 ? P::mx(left, pair[0]) : j == N - 1 ? P::mx(pair[N - 2], right)
+                                                                                   : P::mx(prev[j - 1], pair[j]);
+                    m[j] = P::mx(m[j], P::mn(v, k[j]));
+                }
             }
         } else {
 #pragma unroll
@@ -292,20 +313,17 @@ __device__ __forceinline__ bool sweep(WarpSmem<TH>& sm, int lane, unsigned long 
         }
         hscan<DT, DOWN>(m, k, DOWN ? sm.hLm[r] : sm.hRm[r], lane);
         const uint32_t nw = P::pack(m);
-        const bool ch = nw != old;
-        if (__any_sync(FULL, ch)) {
+        prev_changed = __any_sync(FULL, nw != old);
+        if (prev_changed) {
             sm.tm[r * 32 + lane] = nw;
-            rows_changed |= 1ull << (r - 1);
-            any = true;
-            uint32_t o[N];
-            P::unpack(old, o);
-            col_changed |= (lane == 0 && m[0] != o[0]) || (lane == 31 && m[N - 1] != o[N - 1]);
+            chg |= 1ull << (r - 1);
+            col_changed |= ((nw ^ old) & edge_mask) != 0u;
         }
 #pragma unroll
         for (int j = 0; j < N; ++j) prev[j] = m[j];
+        prev_valid = true;
     }
     __syncwarp();
-    return any;
 }
 
 // --------------------------------------------------------------- tile visit
@@ -333,9 +351,11 @@ __device__ __forceinline__ uint32_t load_word_plain(const unsigned char* row, in
 // store the rows that rose, and report the neighbour tiles to notify: those
 // holding a pixel q next to a pixel p of this tile with
 // marker[q] < min(marker[p], mask[q]) where p's side of the tile rose.
+// `sides` (NB_* bits) names the halo sides whose pixels are new since the
+// tile last converged (all sides on a first visit).
 template <int DT, int CONN, int TH>
 __device__ __noinline__ VisitResult visit_tile(const ImgDesc& d, int tx, int ty, WarpSmem<TH>& sm, int lane,
-                                               unsigned& phase, long long timeout_ns) {
+                                               unsigned& phase, long long timeout_ns, unsigned sides) {
     using P = Px<DT>;
     constexpr int TW = 32 * P::PPW;
     VisitResult res{0u, 0u, true};
@@ -418,15 +438,40 @@ __device__ __noinline__ VisitResult visit_tile(const ImgDesc& d, int tx, int ty,
     }
     __syncwarp();
 
-    // ---- local convergence (MR.cu:320-325, here with full-length scans)
-    unsigned long long rows_changed = 0ull;
+    // ---- local convergence (MR.cu:320-325, here with full-length scans):
+    // raster / anti-raster sweeps until a sweep after the first two changes
+    // nothing.  The first two sweeps also process the rows whose halo
+    // inputs are new: the top row for the raster sweep (N, NW, NE), the
+    // bottom row for the anti-raster sweep (S, SW, SE), every row when a
+    // side column that feeds the sweep changed (W, and E through the
+    // up-right / down-right diagonals for 8-connectivity; the reverse for
+    // the anti-raster sweep).
+    constexpr unsigned long long ALL = TH == 64 ? ~0ull : ((1ull << TH) - 1ull);
+    constexpr unsigned long long TOP = 1ull, BOT = 1ull << (TH - 1);
+    const unsigned side_down = CONN == 8 ? (NB_W | NB_E) : NB_W;
+    const unsigned side_up = CONN == 8 ? (NB_W | NB_E) : NB_E;
+    const unsigned long long force_down = (sides & side_down) ? ALL : (sides & (NB_N | NB_NW | NB_NE)) ? TOP : 0ull;
+    const unsigned long long force_up = (sides & side_up) ? ALL : (sides & (NB_S | NB_SW | NB_SE)) ? BOT : 0ull;
+    const uint32_t edge_mask = lane == 0 ? P::FIRST_MASK : lane == 31 ? P::LAST_MASK : 0u;
+    unsigned long long rows_changed = 0ull, chg_prev = 0ull;
     bool col_changed = false;
     unsigned sweeps = 0;
     for (;;) {
-        const bool ch = (sweeps & 1u) == 0u ? sweep<DT, CONN, TH, true>(sm, lane, rows_changed, col_changed)
-                                            : sweep<DT, CONN, TH, false>(sm, lane, rows_changed, col_changed);
+        unsigned long long dil = chg_prev | (chg_prev << 1) | (chg_prev >> 1);
+        if (sweeps == 0) dil |= force_down;
+        if (sweeps == 1) dil |= force_up;
+        dil &= ALL;
+        unsigned long long chg = 0ull;
+        if (dil != 0ull) {
+            if ((sweeps & 1u) == 0u)
+                sweep<DT, CONN, TH, true>(sm, lane, dil, chg, col_changed, edge_mask);
+            else
+                sweep<DT, CONN, TH, false>(sm, lane, dil, chg, col_changed, edge_mask);
+        }
         ++sweeps;
-        if (!ch && sweeps >= 2) break;
+        rows_changed |= chg;
+        chg_prev = chg;
+        if (chg == 0ull && sweeps >= 2) break;
     }
     res.sweeps = sweeps;
     if (rows_changed == 0ull) return res;  // nothing rose: nothing to store or notify

@@ -26,17 +26,20 @@ __device__ __forceinline__ int find_image(const EngineArgs& a, unsigned g) {
 
 template <int TH>
 __device__ __forceinline__ VisitResult dispatch_visit(const ImgDesc& d, int tx, int ty, WarpSmem<TH>& sm, int lane,
-                                                     unsigned& phase, long long timeout_ns) {
+                                                     unsigned& phase, long long timeout_ns, unsigned sides) {
     const int mode = d.dtype * 2 + (d.conn == 8 ? 1 : 0);
     switch (mode) {
-        case 0: return visit_tile<DT_U8, 4, TH>(d, tx, ty, sm, lane, phase, timeout_ns);
-        case 1: return visit_tile<DT_U8, 8, TH>(d, tx, ty, sm, lane, phase, timeout_ns);
-        case 2: return visit_tile<DT_U16, 4, TH>(d, tx, ty, sm, lane, phase, timeout_ns);
-        case 3: return visit_tile<DT_U16, 8, TH>(d, tx, ty, sm, lane, phase, timeout_ns);
-        case 4: return visit_tile<DT_I32, 4, TH>(d, tx, ty, sm, lane, phase, timeout_ns);
-        default: return visit_tile<DT_I32, 8, TH>(d, tx, ty, sm, lane, phase, timeout_ns);
+        case 0: return visit_tile<DT_U8, 4, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides);
+        case 1: return visit_tile<DT_U8, 8, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides);
+        case 2: return visit_tile<DT_U16, 4, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides);
+        case 3: return visit_tile<DT_U16, 8, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides);
+        case 4: return visit_tile<DT_I32, 4, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides);
+        default: return visit_tile<DT_I32, 8, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides);
     }
 }
+
+// The side of a neighbour tile that faces direction `dir` of this tile.
+__device__ __constant__ static const int kNbOpposite[8] = {1, 0, 3, 2, 7, 6, 5, 4};
 
 struct WarpCounters {
     unsigned long long visits = 0, sweeps = 0, pushes = 0;
@@ -151,7 +154,8 @@ __device__ void notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty, un
         const int nx = tx + kNbDx[lane], ny = ty + kNbDy[lane];
         if (nx >= 0 && nx < d.tiles_x && ny >= 0 && ny < d.tiles_y) {
             gn = (unsigned)d.tile_base + (unsigned)(ny * d.tiles_x + nx);
-            const unsigned old = atomicOr(&a.state[gn], ST_DIRTY);
+            const unsigned old =
+                atomicOr(&a.state[gn], ST_DIRTY | (1u << (ST_SIDE_SHIFT + (unsigned)kNbOpposite[lane])));
             want = (VAR == VAR_UNIQUE || VAR == VAR_ASYNC) ? (old & (ST_DIRTY | ST_ACTIVE)) == 0u : true;
         }
     }
@@ -171,16 +175,18 @@ __device__ bool process_entry(const EngineArgs& a, unsigned g, WarpSmem<TH>& sm,
     if (lane == 0) old = atomicOr(&a.state[g], ST_ACTIVE);
     old = __shfl_sync(FULL, old, 0);
     if (old & ST_ACTIVE) return true;
-    if (lane == 0) old = atomicAnd(&a.state[g], ~ST_DIRTY);
+    if (lane == 0) old = atomicAnd(&a.state[g], ~(ST_DIRTY | ST_SIDES));
     old = __shfl_sync(FULL, old, 0);
     if (old & ST_DIRTY) {
+        unsigned sides = (old & ST_SIDES) >> ST_SIDE_SHIFT;
+        if (sides == 0u) sides = 0xffu;
         __threadfence();  // acquire: neighbours' stores before their DIRTY
         __syncwarp();
         const int ii = find_image(a, g);
         const ImgDesc d = a.imgs[ii];
         const int t = (int)(g - (unsigned)d.tile_base);
         const int ty = t / d.tiles_x, tx = t - ty * d.tiles_x;
-        const VisitResult r = dispatch_visit<TH>(d, tx, ty, sm, lane, phase, a.timeout_ns);
+        const VisitResult r = dispatch_visit<TH>(d, tx, ty, sm, lane, phase, a.timeout_ns, sides);
         if (!r.ok) {
             if (lane == 0) set_error(a.ctrl, DEV_ERR_TIMEOUT);
             return false;
@@ -486,7 +492,7 @@ __global__ void __launch_bounds__(kWarps * 32) engine_kernel(EngineArgs a) {
 __global__ void engine_init_kernel(EngineArgs a, int variant) {
     const unsigned stride = gridDim.x * blockDim.x;
     for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < a.G; g += stride) {
-        a.state[g] = ST_DIRTY;
+        a.state[g] = ST_DIRTY | ST_SIDES;
         if (variant == VAR_MUTEX && g < a.cap) a.q0[g] = a.G - 1u - g;
     }
     if (variant == VAR_ASYNC)

@@ -31,7 +31,9 @@
 
 namespace iwpp {
 
-enum : unsigned { ST_DIRTY = 1u, ST_ACTIVE = 2u };
+// Tile state word: DIRTY, ACTIVE, and (bits 8-15, NB_* << 8) the sides whose
+// halo pixels rose since the tile last converged.
+enum : unsigned { ST_DIRTY = 1u, ST_ACTIVE = 2u, ST_SIDE_SHIFT = 8u, ST_SIDES = 0xffu << 8 };
 enum : int { VAR_MUTEX = 0, VAR_DOUBLE = 1, VAR_UNIQUE = 2, VAR_ASYNC = 3 };
 enum : unsigned { DEV_OK = 0u, DEV_ERR_TIMEOUT = 3u, DEV_ERR_OVERFLOW = 5u };
 
