@@ -70,6 +70,13 @@ typedef struct iwpp_stats {
     int status;          /* iwpp_status of the device run */
     int variant;         /* queue variant used */
     double device_ms;    /* device time of the reconstruction (events) */
+    long long row_steps; /* tile rows processed by the sweeps */
+    /* SM cycles summed over warps per phase, as the reference's clock64
+     * timers (IWPP MP/src/MorphologicalReconstruction.cu:199-206, indices
+     * MorphologicalReconstruction.cuh:9-13): queue read (waiting for and
+     * taking an entry), tile fetch, processing (sweeps), dump (write-back and
+     * neighbour detection), queue write (state updates and insertions). */
+    long long phase_cycles[5];
 } iwpp_stats;
 
 /* One image of a batch. */

@@ -432,6 +432,8 @@ int read_stats(Ctrl* host_ctrl, const Workspace& ws, cudaStream_t s, long long t
         out->status = st;
         out->variant = variant;
         out->device_ms = ms;
+        out->row_steps = (long long)host_ctrl->row_steps;
+        for (int i = 0; i < 5; ++i) out->phase_cycles[i] = (long long)host_ctrl->phase[i];
     }
     return st;
 }
@@ -636,6 +638,8 @@ int iwpp_handle_sync(iwpp_handle h, iwpp_stats* stats) {
         stats->status = st;
         stats->variant = h->last_variant;
         stats->device_ms = ms;
+        stats->row_steps = (long long)c.row_steps;
+        for (int i = 0; i < 5; ++i) stats->phase_cycles[i] = (long long)c.phase[i];
     }
     return set_last(st);
 }
@@ -732,6 +736,8 @@ int iwpp_plan_sync(iwpp_plan p, iwpp_stats* stats) {
         stats->status = st;
         stats->variant = p->variant;
         stats->device_ms = 0.0;
+        stats->row_steps = (long long)c.row_steps;
+        for (int i = 0; i < 5; ++i) stats->phase_cycles[i] = (long long)c.phase[i];
     }
     return set_last(st);
 }

@@ -42,7 +42,8 @@ __device__ __forceinline__ VisitResult dispatch_visit(const ImgDesc& d, int tx, 
 __device__ __constant__ static const int kNbOpposite[8] = {1, 0, 3, 2, 7, 6, 5, 4};
 
 struct WarpCounters {
-    unsigned long long visits = 0, sweeps = 0, pushes = 0;
+    unsigned long long visits = 0, sweeps = 0, pushes = 0, row_steps = 0;
+    long long phase[5] = {0, 0, 0, 0, 0};  // queue read, fetch, processing, dump, queue write
 };
 
 // ---------------------------------------------------------------- mutex
@@ -193,15 +194,23 @@ __device__ bool process_entry(const EngineArgs& a, unsigned g, WarpSmem<TH>& sm,
         }
         cnt.visits += 1;
         cnt.sweeps += r.sweeps;
+        cnt.row_steps += r.row_steps;
+        cnt.phase[1] += r.t_fetch;
+        cnt.phase[2] += r.t_proc;
+        cnt.phase[3] += r.t_dump;
+        const long long q0 = clock64();
         if (r.nb != 0u) {
             __threadfence();  // release: this tile's stores before the neighbours' DIRTY
             __syncwarp();
             notify<VAR>(a, d, tx, ty, r.nb, lane, wq, cnt);
         }
+        cnt.phase[4] += clock64() - q0;
     }
+    const long long q1 = clock64();
     if (lane == 0) old = atomicAnd(&a.state[g], ~ST_ACTIVE);
     old = __shfl_sync(FULL, old, 0);
     if (old & ST_DIRTY) push_entries<VAR>(a, lane == 0, g, lane, wq, cnt);
+    cnt.phase[4] += clock64() - q1;
     return true;
 }
 
@@ -219,6 +228,7 @@ __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
     unsigned ns = 64;
     for (;;) {
         int n = 0, base = 0, verdict = 0;  // verdict: 0 work/retry, 1 exit, 2 refill
+        const long long qr0 = clock64();
         // Test before test-and-set: an idle warp looks at the stack without
         // the lock and takes it only when there is something to take or the
         // job looks finished, so idle pollers never starve a warp that
@@ -286,10 +296,12 @@ __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
             if (ld_volatile(&a.ctrl->error) != 0u) return;
             __nanosleep(ns);
             if (ns < 2048) ns <<= 1;
+            cnt.phase[0] += clock64() - qr0;
             continue;
         }
         idle_since = 0;
         ns = 64;
+        cnt.phase[0] += clock64() - qr0;
         // copy the taken entries out before the lock is released
         unsigned mine = 0u;
         if (lane < n) mine = a.q0[base + lane];
@@ -320,6 +332,7 @@ __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
 template <int TH>
 __device__ void async_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, WarpCounters& cnt, unsigned& phase) {
     for (;;) {
+        const long long qr0 = clock64();
         unsigned p = 0u;
         if (lane == 0) p = atomicAdd(&a.ctrl->ahead, 1u);
         p = __shfl_sync(FULL, p, 0);
@@ -354,8 +367,11 @@ __device__ void async_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
                 }
             }
             verdict = __shfl_sync(FULL, verdict, 0);
+            cnt.phase[0] += clock64() - qr0;
             if (verdict) return;
             g = __shfl_sync(FULL, v, 0) - 1u;
+        } else {
+            cnt.phase[0] += clock64() - qr0;
         }
         const bool ok = process_entry<VAR_ASYNC, TH>(a, g, sm, lane, nullptr, cnt, phase);
         if (lane == 0) {
@@ -443,15 +459,20 @@ __device__ void round_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
         const unsigned* rq = qsel ? a.q1 : a.q0;
         unsigned* wq = qsel ? a.q0 : a.q1;
         for (;;) {
+            const long long qr0 = clock64();
             unsigned idx = 0u;
             if (lane == 0) idx = atomicAdd(&a.ctrl->rcur, 1u);
             idx = __shfl_sync(FULL, idx, 0);
+            cnt.phase[0] += clock64() - qr0;
             if (idx >= rn) break;
             if (ld_volatile(&a.ctrl->error) != 0u) break;
             const unsigned g = vfull ? idx : __ldcg(&rq[idx]);
             if (!process_entry<VAR, TH>(a, g, sm, lane, wq, cnt, phase)) break;
         }
-        if (!grid_barrier_round(a)) return;
+        const long long qb0 = clock64();
+        const bool ok_barrier = grid_barrier_round(a);
+        cnt.phase[0] += clock64() - qb0;
+        if (!ok_barrier) return;
         if (ld_volatile(&a.ctrl->done) != 0u) return;
     }
 }
@@ -482,6 +503,9 @@ __global__ void __launch_bounds__(kWarps * 32) engine_kernel(EngineArgs a) {
         if (cnt.visits) atomicAdd(&a.ctrl->visits, cnt.visits);
         if (cnt.sweeps) atomicAdd(&a.ctrl->sweeps, cnt.sweeps);
         if (cnt.pushes) atomicAdd(&a.ctrl->pushes, cnt.pushes);
+        if (cnt.row_steps) atomicAdd(&a.ctrl->row_steps, cnt.row_steps);
+        for (int i = 0; i < 5; ++i)
+            if (cnt.phase[i] > 0) atomicAdd(&a.ctrl->phase[i], (unsigned long long)cnt.phase[i]);
     }
 }
 
@@ -521,6 +545,8 @@ __global__ void engine_init_kernel(EngineArgs a, int variant) {
         c->visits = 0ull;
         c->sweeps = 0ull;
         c->pushes = 0ull;
+        c->row_steps = 0ull;
+        for (int i = 0; i < 5; ++i) c->phase[i] = 0ull;
     }
 }
 

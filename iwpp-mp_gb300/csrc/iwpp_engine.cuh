@@ -62,7 +62,8 @@ struct Ctrl {
     unsigned long long visits;
     unsigned long long sweeps;
     unsigned long long pushes;
-    unsigned long long pad;
+    unsigned long long row_steps;
+    unsigned long long phase[5];  // cycles: queue read, fetch, processing, dump, queue write
 };
 
 struct EngineArgs {

@@ -52,10 +52,15 @@ class Config(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [("tiles", ctypes.c_longlong), ("visits", ctypes.c_longlong), ("sweeps", ctypes.c_longlong),
                 ("pushes", ctypes.c_longlong), ("rounds", ctypes.c_int), ("restarts", ctypes.c_int),
-                ("status", ctypes.c_int), ("variant", ctypes.c_int), ("device_ms", ctypes.c_double)]
+                ("status", ctypes.c_int), ("variant", ctypes.c_int), ("device_ms", ctypes.c_double),
+                ("row_steps", ctypes.c_longlong), ("phase_cycles", ctypes.c_longlong * 5)]
+
+    PHASES = ("queue_read", "fetch", "processing", "dump", "queue_write")
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "phase_cycles"}
+        d["phase_cycles"] = dict(zip(self.PHASES, list(self.phase_cycles)))
+        return d
 
 
 class Image(ctypes.Structure):
