@@ -297,10 +297,12 @@ __device__ __forceinline__ void sweep(WarpSmem<TH>& sm, int lane, unsigned long 
     P::unpack(sm.tm[(DOWN ? first : first + 2) * 32 + lane], up);
     uint32_t L1 = up[N - 1], L2 = up[N - 1];  // last pixel: most recent / previous row
     uint32_t F1 = up[0], F2 = up[0];          // first pixel: most recent / previous row
-    unsigned long long my_chg = 0ull;
+    unsigned chg_lo = 0u, chg_hi = 0u;
     bool my_col = false;
     const int steps = A * (nrows - 1) + 32;
     int done_rows = nrows;
+    // Every lane runs every step (a divergent branch per step costs more than
+    // the work): an inactive lane computes on a clamped row and discards it.
 #pragma unroll 1
     for (int t = 0; t < steps; ++t) {
         // values of the neighbour lanes as of the end of the previous step
@@ -316,72 +318,84 @@ __device__ __forceinline__ void sweep(WarpSmem<TH>& sm, int lane, unsigned long 
         const int u = t - cp;
         const int kk = A == 2 ? (u >> 1) : u;
         const bool active = u >= 0 && (A == 1 || (u & 1) == 0) && kk < nrows;
-        if (active) {
-            const int i = DOWN ? first + kk : first - kk;  // tile row
-            const int r = i + 1;                           // SMEM row
-            const int rp = DOWN ? r - 1 : r + 1;           // SMEM row before it
-            const uint32_t old = sm.tm[r * 32 + lane];
-            uint32_t m[N], k[N];
-            P::unpack(old, m);
-            P::unpack(sm.tk[r * 32 + lane], k);
-            // previous pixel in scan order, and the diagonal inputs
-            uint32_t along, diag_a, diag_b;  // diag_a / diag_b: before / after side of the previous row
-            if (DOWN) {
-                along = lane == 0 ? sm.hLm[r] : lL1;
-                diag_a = lane == 0 ? sm.hLm[rp] : lL2;   // up-left
-                diag_b = lane == 31 ? sm.hRm[rp] : rF1;  // up-right (lane c+1, one step earlier)
-            } else {
-                along = lane == 31 ? sm.hRm[r] : rF1;
-                diag_a = lane == 31 ? sm.hRm[rp] : rF2;  // down-right
-                diag_b = lane == 0 ? sm.hLm[rp] : lL1;   // down-left (lane c-1, one step earlier)
-            }
-#pragma unroll
-            for (int s = 0; s < N; ++s) {
-                const int j = DOWN ? s : N - 1 - s;
-                uint32_t v = up[j];
-                if (CONN == 8) {
-                    const uint32_t lft = j == 0 ? (DOWN ? diag_a : diag_b) : up[j - 1];
-                    const uint32_t rgt = j == N - 1 ? (DOWN ? diag_b : diag_a) : up[j + 1];
-                    v = P::mx3(lft, v, rgt);
-                }
-                const uint32_t prevpx = s == 0 ? along : m[DOWN ? j - 1 : j + 1];
-                v = P::mx(v, prevpx);
-                m[j] = P::mx(m[j], P::mn(v, k[j]));
-            }
-            const uint32_t nw = P::pack(m);
-            if (nw != old) {
-                sm.tm[r * 32 + lane] = nw;
-                my_chg |= 1ull << i;
-                my_col |= ((nw ^ old) & edge_mask) != 0u;
-            }
-#pragma unroll
-            for (int j = 0; j < N; ++j) up[j] = m[j];
-            L2 = L1;
-            F2 = F1;
-            L1 = m[N - 1];
-            F1 = m[0];
+        const int kc = min(max(kk, 0), nrows - 1);
+        const int i = DOWN ? first + kc : first - kc;  // tile row
+        const int r = i + 1;                           // SMEM row
+        const int rp = DOWN ? r - 1 : r + 1;           // SMEM row before it
+        const uint32_t old = sm.tm[r * 32 + lane];
+        uint32_t m[N], k[N];
+        P::unpack(old, m);
+        P::unpack(sm.tk[r * 32 + lane], k);
+        // previous pixel in scan order, and the diagonal inputs
+        uint32_t along, diag_a, diag_b;  // diag_a / diag_b: before / after side of the previous row
+        if (DOWN) {
+            along = lane == 0 ? sm.hLm[r] : lL1;
+            diag_a = lane == 0 ? sm.hLm[rp] : lL2;   // up-left
+            diag_b = lane == 31 ? sm.hRm[rp] : rF1;  // up-right (lane c+1, one step earlier)
+        } else {
+            along = lane == 31 ? sm.hRm[r] : rF1;
+            diag_a = lane == 31 ? sm.hRm[rp] : rF2;  // down-right
+            diag_b = lane == 0 ? sm.hLm[rp] : lL1;   // down-left (lane c-1, one step earlier)
         }
+        // b_j = max(m_j, min(vertical_j, k_j)); p = in-word prefix without
+        // the carry; K = prefix minimum of the mask.  The carry `along` then
+        // enters every pixel at once: m_j = max(p_j, min(along, K_j)).
+        uint32_t p[N], K[N];
+#pragma unroll
+        for (int s = 0; s < N; ++s) {
+            const int j = DOWN ? s : N - 1 - s;
+            uint32_t v = up[j];
+            if (CONN == 8) {
+                const uint32_t lft = j == 0 ? (DOWN ? diag_a : diag_b) : up[j - 1];
+                const uint32_t rgt = j == N - 1 ? (DOWN ? diag_b : diag_a) : up[j + 1];
+                v = P::mx3(lft, v, rgt);
+            }
+            const uint32_t b = P::mx(m[j], P::mn(v, k[j]));
+            if (s == 0) {
+                p[j] = b;
+                K[j] = k[j];
+            } else {
+                const int jp = DOWN ? j - 1 : j + 1;
+                p[j] = P::mx(b, P::mn(p[jp], k[j]));
+                K[j] = P::mn(K[jp], k[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < N; ++j) m[j] = P::mx(p[j], P::mn(along, K[j]));
+        const uint32_t nw = P::pack(m);
+        const bool ch = active && nw != old;
+        if (ch) sm.tm[r * 32 + lane] = nw;
+        chg_lo |= (ch && i < 32) ? (1u << (i & 31)) : 0u;
+        chg_hi |= (ch && i >= 32) ? (1u << (i & 31)) : 0u;
+        my_col |= ch && ((nw ^ old) & edge_mask) != 0u;
+#pragma unroll
+        for (int j = 0; j < N; ++j) up[j] = active ? m[j] : up[j];
+        L2 = active ? L1 : L2;
+        F2 = active ? F1 : F2;
+        L1 = active ? m[N - 1] : L1;
+        F1 = active ? m[0] : F1;
         // lane 31 (raster) / lane 0 (anti-raster) has just finished row
         // `first +- kk_end`; stop once such a row past the last dirty row is
         // unchanged in every lane.
-        const int kk_end = A == 2 ? ((t - 31) >> 1) : t - 31;
-        if (t >= 31 && (A == 1 || ((t - 31) & 1) == 0) && kk_end < nrows) {
+        const int ue = t - 31;
+        const int kk_end = A == 2 ? (ue >> 1) : ue;
+        if (ue >= 0 && (A == 1 || (ue & 1) == 0) && kk_end < nrows) {
             const int i_end = DOWN ? first + kk_end : first - kk_end;
             const bool past = DOWN ? i_end > last_dirty : i_end < last_dirty;
-            if (past && __ballot_sync(FULL, (my_chg >> i_end) & 1ull) == 0u) {
+            const unsigned bit = (i_end < 32 ? chg_lo : chg_hi) >> (i_end & 31);
+            if (past && __ballot_sync(FULL, bit & 1u) == 0u) {
                 done_rows = kk_end + 1;
                 break;
             }
         }
     }
     // OR the per-lane row masks over the warp
-    unsigned lo32 = (unsigned)my_chg, hi32 = (unsigned)(my_chg >> 32);
 #pragma unroll
     for (int d = 16; d >= 1; d >>= 1) {
-        lo32 |= __shfl_xor_sync(FULL, lo32, d);
-        hi32 |= __shfl_xor_sync(FULL, hi32, d);
+        chg_lo |= __shfl_xor_sync(FULL, chg_lo, d);
+        chg_hi |= __shfl_xor_sync(FULL, chg_hi, d);
     }
-    chg = ((unsigned long long)hi32 << 32) | lo32;
+    chg = ((unsigned long long)chg_hi << 32) | chg_lo;
     col_changed |= my_col;
     row_steps += (unsigned)done_rows;
     __syncwarp();
