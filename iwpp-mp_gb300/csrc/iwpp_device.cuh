@@ -262,142 +262,68 @@ __device__ __forceinline__ void hscan(uint32_t (&m)[Px<DT>::PPW], const uint32_t
 // its constraints towards N+ = {left, up-left, up, up-right}; after an
 // anti-raster sweep towards N-.
 //
-// Skewed wavefront.  Lane c processes tile row i at step A * k + c' where k
-// is the row's position in sweep order and c' = c (raster) or 31 - c
-// (anti-raster); A = 1 for 4-connectivity and 2 for 8-connectivity.  Then
-// every input of a pixel was produced one to three steps earlier by the
-// same lane (the row before) or a neighbour lane (the pixel before in the
-// row, and the diagonal pixels of the row before), so a step is a couple of
-// shuffles and a short in-word chain: no per-row warp scan and no vote.
-// With A = 2 the up-right input (raster) of lane c comes from lane c+1's row
-// one step earlier, which is why 8-connectivity needs two steps per row.
-//
-// Rows before the first dirty row (in sweep order) are not processed; the
-// sweep stops once a whole row past the last dirty row came through
-// unchanged (all later rows then see the inputs they already satisfied).
-// `dil` = rows that must be processed (dilated changes of the previous
-// sweep and rows with new halo inputs); `chg` receives the rows that rose
-// (bit i for tile row i = SMEM row i + 1).
+// Rows are skipped when nothing they depend on can have changed since they
+// last satisfied this sweep's constraints: a row is processed when the row
+// before it (in sweep order) rose in this sweep, or when it or a vertical
+// neighbour rose in the previous sweep (`dil`, already dilated by one row),
+// or when its halo inputs are new (`force`, folded into `dil` by the caller).
+// `chg` receives the rows that rose (bit r-1 for SMEM row r).
 template <int DT, int CONN, int TH, bool DOWN>
 __device__ __forceinline__ void sweep(WarpSmem<TH>& sm, int lane, unsigned long long dil, unsigned long long& chg,
                                       bool& col_changed, uint32_t edge_mask, unsigned& row_steps) {
     using P = Px<DT>;
     constexpr int N = P::PPW;
-    constexpr int A = CONN == 8 ? 2 : 1;
-    // first / last row to process, in tile-row indices
-    const int lo = __ffsll((long long)dil) - 1;
-    const int hi = 63 - __clzll((long long)dil);
-    const int first = DOWN ? lo : hi;          // first row in sweep order
-    const int last_dirty = DOWN ? hi : lo;     // after it, an unchanged row ends the sweep
-    const int nrows = DOWN ? TH - lo : hi + 1; // rows from `first` to the tile edge
-    const int cp = DOWN ? lane : 31 - lane;    // lane position in sweep order
-
-    // inputs from the row before `first` (SMEM row first, or first + 2)
-    uint32_t up[N];
-    P::unpack(sm.tm[(DOWN ? first : first + 2) * 32 + lane], up);
-    uint32_t L1 = up[N - 1], L2 = up[N - 1];  // last pixel: most recent / previous row
-    uint32_t F1 = up[0], F2 = up[0];          // first pixel: most recent / previous row
-    unsigned chg_lo = 0u, chg_hi = 0u;
-    bool my_col = false;
-    const int steps = A * (nrows - 1) + 32;
-    int done_rows = nrows;
-    // Every lane runs every step (a divergent branch per step costs more than
-    // the work): an inactive lane computes on a clamped row and discards it.
+    uint32_t prev[N];
+    bool prev_valid = false, prev_changed = false;
 #pragma unroll 1
-    for (int t = 0; t < steps; ++t) {
-        // values of the neighbour lanes as of the end of the previous step
-        const uint32_t lL1 = __shfl_up_sync(FULL, L1, 1);
-        const uint32_t rF1 = __shfl_down_sync(FULL, F1, 1);
-        uint32_t lL2 = 0u, rF2 = 0u;
-        if (CONN == 8) {
-            if (DOWN)
-                lL2 = __shfl_up_sync(FULL, L2, 1);
-            else
-                rF2 = __shfl_down_sync(FULL, F2, 1);
+    for (int i = 0; i < TH; ++i) {
+        const int r = DOWN ? 1 + i : TH - i;  // SMEM row
+        const int rp = DOWN ? r - 1 : r + 1;  // SMEM row before it in sweep order
+        if (!prev_changed && !((dil >> (r - 1)) & 1ull)) {
+            prev_valid = false;
+            continue;
         }
-        const int u = t - cp;
-        const int kk = A == 2 ? (u >> 1) : u;
-        const bool active = u >= 0 && (A == 1 || (u & 1) == 0) && kk < nrows;
-        const int kc = min(max(kk, 0), nrows - 1);
-        const int i = DOWN ? first + kc : first - kc;  // tile row
-        const int r = i + 1;                           // SMEM row
-        const int rp = DOWN ? r - 1 : r + 1;           // SMEM row before it
+        if (!prev_valid) P::unpack(sm.tm[rp * 32 + lane], prev);
+        ++row_steps;
         const uint32_t old = sm.tm[r * 32 + lane];
         uint32_t m[N], k[N];
         P::unpack(old, m);
         P::unpack(sm.tk[r * 32 + lane], k);
-        // previous pixel in scan order, and the diagonal inputs
-        uint32_t along, diag_a, diag_b;  // diag_a / diag_b: before / after side of the previous row
-        if (DOWN) {
-            along = lane == 0 ? sm.hLm[r] : lL1;
-            diag_a = lane == 0 ? sm.hLm[rp] : lL2;   // up-left
-            diag_b = lane == 31 ? sm.hRm[rp] : rF1;  // up-right (lane c+1, one step earlier)
-        } else {
-            along = lane == 31 ? sm.hRm[r] : rF1;
-            diag_a = lane == 31 ? sm.hRm[rp] : rF2;  // down-right
-            diag_b = lane == 0 ? sm.hLm[rp] : lL1;   // down-left (lane c-1, one step earlier)
-        }
-        // b_j = max(m_j, min(vertical_j, k_j)); p = in-word prefix without
-        // the carry; K = prefix minimum of the mask.  The carry `along` then
-        // enters every pixel at once: m_j = max(p_j, min(along, K_j)).
-        uint32_t p[N], K[N];
-#pragma unroll
-        for (int s = 0; s < N; ++s) {
-            const int j = DOWN ? s : N - 1 - s;
-            uint32_t v = up[j];
-            if (CONN == 8) {
-                const uint32_t lft = j == 0 ? (DOWN ? diag_a : diag_b) : up[j - 1];
-                const uint32_t rgt = j == N - 1 ? (DOWN ? diag_b : diag_a) : up[j + 1];
-                v = P::mx3(lft, v, rgt);
-            }
-            const uint32_t b = P::mx(m[j], P::mn(v, k[j]));
-            if (s == 0) {
-                p[j] = b;
-                K[j] = k[j];
+        if (CONN == 8) {
+            uint32_t left = __shfl_up_sync(FULL, prev[N - 1], 1);
+            uint32_t right = __shfl_down_sync(FULL, prev[0], 1);
+            if (lane == 0) left = sm.hLm[rp];
+            if (lane == 31) right = sm.hRm[rp];
+            if (N == 1) {
+                m[0] = P::mx(m[0], P::mn(P::mx3(left, prev[0], right), k[0]));
             } else {
-                const int jp = DOWN ? j - 1 : j + 1;
-                p[j] = P::mx(b, P::mn(p[jp], k[j]));
-                K[j] = P::mn(K[jp], k[j]);
-            }
-        }
+                // shared pairwise maxima of the previous row
+                uint32_t pair[N > 1 ? N - 1 : 1];
 #pragma unroll
-        for (int j = 0; j < N; ++j) m[j] = P::mx(p[j], P::mn(along, K[j]));
+                for (int j = 0; j + 1 < N; ++j) pair[j] = P::mx(prev[j], prev[j + 1]);
+#pragma unroll
+                for (int j = 0; j < N; ++j) {
+                    const uint32_t v = j == 0 ? P::mx(left, pair[0]) : j == N - 1 ? P::mx(pair[N - 2], right)
+                                                                                   : P::mx(prev[j - 1], pair[j]);
+                    m[j] = P::mx(m[j], P::mn(v, k[j]));
+                }
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < N; ++j) m[j] = P::mx(m[j], P::mn(prev[j], k[j]));
+        }
+        hscan<DT, DOWN>(m, k, DOWN ? sm.hLm[r] : sm.hRm[r], lane);
         const uint32_t nw = P::pack(m);
-        const bool ch = active && nw != old;
-        if (ch) sm.tm[r * 32 + lane] = nw;
-        chg_lo |= (ch && i < 32) ? (1u << (i & 31)) : 0u;
-        chg_hi |= (ch && i >= 32) ? (1u << (i & 31)) : 0u;
-        my_col |= ch && ((nw ^ old) & edge_mask) != 0u;
-#pragma unroll
-        for (int j = 0; j < N; ++j) up[j] = active ? m[j] : up[j];
-        L2 = active ? L1 : L2;
-        F2 = active ? F1 : F2;
-        L1 = active ? m[N - 1] : L1;
-        F1 = active ? m[0] : F1;
-        // lane 31 (raster) / lane 0 (anti-raster) has just finished row
-        // `first +- kk_end`; stop once such a row past the last dirty row is
-        // unchanged in every lane.
-        const int ue = t - 31;
-        const int kk_end = A == 2 ? (ue >> 1) : ue;
-        if (ue >= 0 && (A == 1 || (ue & 1) == 0) && kk_end < nrows) {
-            const int i_end = DOWN ? first + kk_end : first - kk_end;
-            const bool past = DOWN ? i_end > last_dirty : i_end < last_dirty;
-            const unsigned bit = (i_end < 32 ? chg_lo : chg_hi) >> (i_end & 31);
-            if (past && __ballot_sync(FULL, bit & 1u) == 0u) {
-                done_rows = kk_end + 1;
-                break;
-            }
+        prev_changed = __any_sync(FULL, nw != old);
+        if (prev_changed) {
+            sm.tm[r * 32 + lane] = nw;
+            chg |= 1ull << (r - 1);
+            col_changed |= ((nw ^ old) & edge_mask) != 0u;
         }
-    }
-    // OR the per-lane row masks over the warp
 #pragma unroll
-    for (int d = 16; d >= 1; d >>= 1) {
-        chg_lo |= __shfl_xor_sync(FULL, chg_lo, d);
-        chg_hi |= __shfl_xor_sync(FULL, chg_hi, d);
+        for (int j = 0; j < N; ++j) prev[j] = m[j];
+        prev_valid = true;
     }
-    chg = ((unsigned long long)chg_hi << 32) | chg_lo;
-    col_changed |= my_col;
-    row_steps += (unsigned)done_rows;
     __syncwarp();
 }
 

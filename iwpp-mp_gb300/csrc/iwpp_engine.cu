@@ -144,11 +144,14 @@ __device__ void push_entries(const EngineArgs& a, bool want, unsigned gn, int la
     cnt.pushes += (unsigned)n;
 }
 
-// Marks the neighbour tiles in `nb` DIRTY and inserts them (VAR_UNIQUE:
-// only those that were neither pending nor being visited).
+// Marks the neighbour tiles in `nb` DIRTY and inserts them (VAR_UNIQUE /
+// VAR_ASYNC: only those that were neither pending nor being visited).  With
+// the async queue one of the newly dirty tiles is not inserted but returned:
+// the warp visits it next itself, following the propagation front without a
+// trip through the queue.  Returns ~0u when there is none.
 template <int VAR>
-__device__ void notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty, unsigned nb, int lane, unsigned* wq,
-                       WarpCounters& cnt) {
+__device__ unsigned notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty, unsigned nb, int lane, unsigned* wq,
+                           WarpCounters& cnt) {
     bool want = false;
     unsigned gn = 0u;
     if (lane < 8 && ((nb >> lane) & 1u)) {
@@ -160,7 +163,17 @@ __device__ void notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty, un
             want = (VAR == VAR_UNIQUE || VAR == VAR_ASYNC) ? (old & (ST_DIRTY | ST_ACTIVE)) == 0u : true;
         }
     }
+    unsigned cont = ~0u;
+    if (VAR == VAR_ASYNC) {
+        const unsigned ballot = __ballot_sync(FULL, want);
+        if (ballot != 0u) {
+            const int leader = __ffs(ballot) - 1;
+            cont = __shfl_sync(FULL, gn, leader);
+            if (lane == leader) want = false;
+        }
+    }
     push_entries<VAR>(a, want, gn, lane, wq, cnt);
+    return cont;
 }
 
 // ------------------------------------------------------------ one entry
@@ -171,7 +184,8 @@ __device__ void notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty, un
 // revisited at once with half-updated neighbours.
 template <int VAR, int TH>
 __device__ bool process_entry(const EngineArgs& a, unsigned g, WarpSmem<TH>& sm, int lane, unsigned* wq,
-                              WarpCounters& cnt, unsigned& phase) {
+                              WarpCounters& cnt, unsigned& phase, unsigned* next = nullptr) {
+    if (next) *next = ~0u;
     unsigned old = 0u;
     if (lane == 0) old = atomicOr(&a.state[g], ST_ACTIVE);
     old = __shfl_sync(FULL, old, 0);
@@ -202,7 +216,8 @@ __device__ bool process_entry(const EngineArgs& a, unsigned g, WarpSmem<TH>& sm,
         if (r.nb != 0u) {
             __threadfence();  // release: this tile's stores before the neighbours' DIRTY
             __syncwarp();
-            notify<VAR>(a, d, tx, ty, r.nb, lane, wq, cnt);
+            const unsigned cont = notify<VAR>(a, d, tx, ty, r.nb, lane, wq, cnt);
+            if (next) *next = cont;
         }
         cnt.phase[4] += clock64() - q0;
     }
@@ -353,7 +368,7 @@ __device__ void async_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
                         break;
                     }
                     __nanosleep(ns);
-                    if (ns < 2048) ns <<= 1;
+                    if (ns < 256) ns <<= 1;
                     const unsigned prog = ld_volatile(&a.ctrl->progress);
                     const long long now = globaltimer_ns();
                     if (prog != idle_progress) {
@@ -373,7 +388,15 @@ __device__ void async_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
         } else {
             cnt.phase[0] += clock64() - qr0;
         }
-        const bool ok = process_entry<VAR_ASYNC, TH>(a, g, sm, lane, nullptr, cnt, phase);
+        // visit the entry, then keep following the front while the visits
+        // leave a newly dirty neighbour behind
+        bool ok = true;
+        for (;;) {
+            unsigned nxt = ~0u;
+            ok = process_entry<VAR_ASYNC, TH>(a, g, sm, lane, nullptr, cnt, phase, &nxt);
+            if (!ok || nxt == ~0u) break;
+            g = nxt;
+        }
         if (lane == 0) {
             __threadfence();
             atomicAdd(&a.ctrl->progress, 1u);
