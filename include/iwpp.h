@@ -32,7 +32,9 @@ typedef enum iwpp_status {
     IWPP_ERR_CUDA = 4,      /* a CUDA runtime call failed */
     IWPP_ERR_OVERFLOW = 5,  /* queue overflowed more often than max_restarts */
     IWPP_ERR_NO_DEVICE = 6, /* no CUDA device, or not a GB300-class (sm_103) one */
-    IWPP_ERR_BUSY = 7       /* a server is full or shutting down */
+    IWPP_ERR_BUSY = 7,      /* a server is full or shutting down */
+    IWPP_ERR_TOO_LARGE = 8  /* the image needs more workspace than the static scratch of
+                               iwpp_reconstruct_noalloc holds */
 } iwpp_status;
 
 typedef enum iwpp_dtype { IWPP_U8 = 0, IWPP_U16 = 1, IWPP_I32 = 2 } iwpp_dtype;
@@ -148,6 +150,28 @@ IWPP_API int iwpp_sweep(void *marker, const void *mask, size_t pitch_marker, siz
  * floats. */
 IWPP_API int iwpp_sweep_timing(void *marker, const void *mask, size_t pitch_marker, size_t pitch_mask, int width,
                                int height, int dtype, int connectivity, float *ms_out);
+
+/* ---- reconstruction that allocates nothing ----------------------------- */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * where they reconstruct -- e.g. a framework whose caching allocator owns
+ * the device memory budget, or a latency-critical loop that cannot afford
+ * the device-wide synchronisation of cudaMalloc / cudaFree.  The caller
+ * passes device marker / mask buffers (rows 4-byte aligned, any pitch,
+ * uint8 / uint16 / int32, 4- or 8-connectivity); the queues, tile states and
+ * counters live in a static device array of IWPP_NOALLOC_SCRATCH_BYTES that
+ * every GPU loading the library keeps until the process exits.  It holds
+ * images up to about 340 000 tiles (e.g. 32768 x 32768 uint8, 16384 x 16384
+ * int32); larger images return IWPP_ERR_TOO_LARGE.  Uses the async queue,
+ * 64-row tiles, plain loads; synchronous on `stream` (NULL = legacy default
+ * stream).  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls share the one array: calls whose
+ * work overlaps on the GPU (concurrent host threads or streams) race and
+ * must be serialised by the caller.  Each call clears the state it needs;
+ * the array otherwise keeps the last call's contents. */
+#define IWPP_NOALLOC_SCRATCH_BYTES (4u << 20)
+IWPP_API int iwpp_reconstruct_noalloc(void *marker, const void *mask, size_t pitch_marker, size_t pitch_mask,
+                                      int width, int height, int dtype, int connectivity, void *stream);
 
 /* ---- reference-compatible entry points --------------------------------- */
 /* Exactly the reference signature (IWPP MP/include/MorphologicalReconstruction.cuh:45-46;

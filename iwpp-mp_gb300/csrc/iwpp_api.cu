@@ -522,6 +522,7 @@ const char* iwpp_status_string(int status) {
         case IWPP_ERR_OVERFLOW: return "queue overflow restarts exhausted";
         case IWPP_ERR_NO_DEVICE: return "no sm_103 (GB300) CUDA device";
         case IWPP_ERR_BUSY: return "server full or shutting down";
+        case IWPP_ERR_TOO_LARGE: return "image too large for the no-allocation scratch";
         default: return "unknown status";
     }
 }

@@ -28,7 +28,7 @@ VARIANTS = {"mutex": MUTEX, "mp": MUTEX, "double": DOUBLE, "dq": DOUBLE, "unique
             "async": ASYNC, "default": DEFAULT}
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "timeout", 4: "CUDA error",
-          5: "queue overflow restarts exhausted", 6: "no sm_103 device", 7: "busy"}
+          5: "queue overflow restarts exhausted", 6: "no sm_103 device", 7: "busy", 8: "too large for the scratch"}
 
 
 class IwppError(RuntimeError):
@@ -100,6 +100,9 @@ _SIGS = {
     "iwpp_sweep_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
                                          ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_float)]),
+    "iwpp_reconstruct_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
+                                                ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                ctypes.c_void_p]),
     "MorphologicalReconstruction": (None, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
                                            ctypes.c_int]),
     "configureHeapSize": (None, []),
