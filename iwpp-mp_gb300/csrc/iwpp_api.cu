@@ -182,10 +182,13 @@ long long queue_capacity_for(int variant, long long G, long long requested) {
 struct Staged {
     void* user_marker;
     size_t user_pm;
+    const void* user_mask;
+    size_t user_pk;
     void* buf_m;  // staging copies (nullptr when the user buffer is used)
     void* buf_k;
     size_t pitch;
     int w, h, dtype;
+    bool owned;   // allocated for a plan: copied and freed by the plan
 };
 
 struct Job {
@@ -199,8 +202,14 @@ struct Job {
     Config cfg;
 };
 
+// How images whose rows are not 4-byte aligned are handled.
+enum StageMode { STAGE_REJECT = 0, STAGE_ASYNC = 1, STAGE_OWNED = 2 };
+
+// STAGE_ASYNC: stream-ordered staging buffers, copied in now and back by
+// finish_staging.  STAGE_OWNED: plain allocations owned by the caller (a
+// plan), copies left to the caller.
 int build_job(Job& job, const iwpp_image* imgs, int n, int variant, const iwpp_config* cfgp, cudaStream_t s,
-              bool allow_staging) {
+              int staging) {
     job.cfg = resolve_config(cfgp);
     job.variant = resolve_variant(variant);
     int th = job.cfg.tile_rows;
@@ -230,16 +239,47 @@ int build_job(Job& job, const iwpp_image* imgs, int n, int variant, const iwpp_c
         d.tiles_y = (im.height + th - 1) / th;
         d.tile_rows = th;
         d.tile_base = (int)G;
-        Staged st{im.marker, im.pitch_marker, nullptr, nullptr, 0, im.width, im.height, im.dtype};
+        Staged st{im.marker, im.pitch_marker, im.mask, im.pitch_mask, nullptr, nullptr, 0, im.width, im.height,
+                  im.dtype, staging == STAGE_OWNED};
         const bool ok_m = aligned_for_engine(im.marker, im.pitch_marker);
         const bool ok_k = aligned_for_engine(im.mask, im.pitch_mask);
         if (!ok_m || !ok_k) {
-            if (!allow_staging) return IWPP_ERR_INVALID;
+            if (staging == STAGE_REJECT) return IWPP_ERR_INVALID;
             // Rows that do not start on a 4-byte boundary: reconstruct in
             // aligned copies and copy the marker back afterwards.
             const size_t row = (size_t)im.width * bpp_of(im.dtype);
             const size_t pitch = align_up(row, 128);
-            cudaError_t e = cudaMallocAsync(&st.buf_m, pitch * im.height, s);
+            cudaError_t e;
+            if (staging == STAGE_OWNED) {
+                e = cudaMalloc(&st.buf_m, pitch * im.height);
+                if (e == cudaSuccess) e = cudaMalloc(&st.buf_k, pitch * im.height);
+                if (e != cudaSuccess) {
+                    if (st.buf_m) cudaFree(st.buf_m);
+                    cudaGetLastError();
+                    return cuda_status(e);
+                }
+                st.pitch = pitch;
+                job.staged.push_back(st);  // recorded even if a later image fails
+                st.buf_m = st.buf_k = nullptr;
+                Staged& kept = job.staged.back();
+                d.marker = static_cast<unsigned char*>(kept.buf_m);
+                d.mask = static_cast<const unsigned char*>(kept.buf_k);
+                d.pitch_m = (long long)pitch;
+                d.pitch_k = (long long)pitch;
+                G += (long long)d.tiles_x * d.tiles_y;
+                if (G > 0x7fffffffll) return IWPP_ERR_INVALID;
+                CUtensorMap maps2[2];
+                std::memset(maps2, 0, sizeof(maps2));
+                const bool tma2 = !job.cfg.plain_loads &&
+                                  encode_tmap(&maps2[0], d.marker, d.W, d.H, pitch, bpp_of(d.dtype), th) &&
+                                  encode_tmap(&maps2[1], d.mask, d.W, d.H, pitch, bpp_of(d.dtype), th);
+                job.tmaps.push_back(maps2[0]);
+                job.tmaps.push_back(maps2[1]);
+                job.has_tma.push_back(tma2 ? 1 : 0);
+                job.descs.push_back(d);
+                continue;
+            }
+            e = cudaMallocAsync(&st.buf_m, pitch * im.height, s);
             if (e == cudaSuccess) e = cudaMallocAsync(&st.buf_k, pitch * im.height, s);
             if (e == cudaSuccess)
                 e = cudaMemcpy2DAsync(st.buf_m, pitch, im.marker, im.pitch_marker, row, im.height,
@@ -278,7 +318,7 @@ int build_job(Job& job, const iwpp_image* imgs, int n, int variant, const iwpp_c
 int finish_staging(Job& job, cudaStream_t s) {
     cudaError_t first = cudaSuccess;
     for (auto& st : job.staged) {
-        if (!st.buf_m) continue;
+        if (!st.buf_m || st.owned) continue;
         const size_t row = (size_t)st.w * bpp_of(st.dtype);
         cudaError_t e = cudaMemcpy2DAsync(st.user_marker, st.user_pm, st.buf_m, st.pitch, row, st.h,
                                           cudaMemcpyDeviceToDevice, s);
@@ -307,6 +347,7 @@ struct iwpp_handle_s {
 
 struct iwpp_plan_s {
     iwpp_handle h = nullptr;
+    std::vector<Staged> staged;  // owned staging buffers of unaligned images
     Workspace ws;
     Ctrl* host_ctrl = nullptr;
     cudaGraph_t graph = nullptr;
@@ -487,7 +528,7 @@ int run_job_sync(iwpp_handle h, const iwpp_image* imgs, int n, int variant, cons
     cudaGetDevice(&prev_dev);
     if (prev_dev != h->device) cudaSetDevice(h->device);
     Job job;
-    rc = build_job(job, imgs, n, variant, cfg, s, true);
+    rc = build_job(job, imgs, n, variant, cfg, s, STAGE_ASYNC);
     if (rc == IWPP_OK) rc = enqueue_job(job, h->ws, s, h->device, true, h->ev0, h->ev1, true);
     const int rc_stage = finish_staging(job, s);
     if (rc == IWPP_OK) {
@@ -600,7 +641,7 @@ int iwpp_reconstruct_async(iwpp_handle h, void* marker, const void* mask, size_t
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     iwpp_image im{marker, mask, pitch_marker, pitch_mask, width, height, dtype, connectivity};
     Job job;
-    int rc = build_job(job, &im, 1, variant, cfg, s, true);
+    int rc = build_job(job, &im, 1, variant, cfg, s, STAGE_ASYNC);
     if (rc == IWPP_OK) rc = enqueue_job(job, h->ws, s, h->device, true, h->ev0, h->ev1, true);
     const int rc2 = finish_staging(job, s);
     if (rc == IWPP_OK) rc = rc2;
@@ -658,7 +699,9 @@ int iwpp_plan_create(iwpp_plan* out, iwpp_handle h, const iwpp_image* images, in
     p->h = h;
     Job job;
     cudaStream_t cs = nullptr;
-    int rc = build_job(job, images, n, variant, cfg, nullptr, false);
+    int rc = build_job(job, images, n, variant, cfg, nullptr, STAGE_OWNED);
+    for (const auto& st : job.staged)
+        if (st.owned && st.buf_m) p->staged.push_back(st);
     cudaError_t e = cudaSuccess;
     if (rc == IWPP_OK) {
         p->tiles = job.G;
@@ -693,7 +736,24 @@ int iwpp_plan_create(iwpp_plan* out, iwpp_handle h, const iwpp_image* images, in
         e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
         rc = cuda_status(e);
         if (rc == IWPP_OK) {
-            rc = enqueue_job(job, p->ws, cs, h->device, false, nullptr, nullptr, false);
+            // unaligned images: copy into the plan's staging buffers, run, copy back
+            for (const auto& st : p->staged) {
+                const size_t row = (size_t)st.w * bpp_of(st.dtype);
+                if (e == cudaSuccess)
+                    e = cudaMemcpy2DAsync(st.buf_m, st.pitch, st.user_marker, st.user_pm, row, st.h,
+                                          cudaMemcpyDeviceToDevice, cs);
+                if (e == cudaSuccess)
+                    e = cudaMemcpy2DAsync(st.buf_k, st.pitch, st.user_mask, st.user_pk, row, st.h,
+                                          cudaMemcpyDeviceToDevice, cs);
+            }
+            rc = cuda_status(e);
+            if (rc == IWPP_OK) rc = enqueue_job(job, p->ws, cs, h->device, false, nullptr, nullptr, false);
+            for (const auto& st : p->staged) {
+                const size_t row = (size_t)st.w * bpp_of(st.dtype);
+                if (rc == IWPP_OK)
+                    rc = cuda_status(cudaMemcpy2DAsync(st.user_marker, st.user_pm, st.buf_m, st.pitch, row, st.h,
+                                                       cudaMemcpyDeviceToDevice, cs));
+            }
             cudaError_t e2 = cudaStreamEndCapture(cs, &p->graph);
             if (rc == IWPP_OK) rc = cuda_status(e2);
         }
@@ -749,6 +809,10 @@ int iwpp_plan_destroy(iwpp_plan p) {
     if (p->graph) cudaGraphDestroy(p->graph);
     if (p->ws.base) cudaFree(p->ws.base);
     if (p->host_ctrl) cudaFreeHost(p->host_ctrl);
+    for (auto& st : p->staged) {
+        if (st.buf_m) cudaFree(st.buf_m);
+        if (st.buf_k) cudaFree(st.buf_k);
+    }
     delete p;
     return IWPP_OK;
 }
@@ -773,7 +837,7 @@ int iwpp_clip(void* marker, const void* mask, size_t pitch_marker, size_t pitch_
         Job job;
         cudaStream_t s = static_cast<cudaStream_t>(stream);
         iwpp_config c{};
-        rc = build_job(job, &im, 1, IWPP_QUEUE_UNIQUE, &c, s, true);
+        rc = build_job(job, &im, 1, IWPP_QUEUE_UNIQUE, &c, s, STAGE_ASYNC);
         if (rc == IWPP_OK && !job.descs.empty()) rc = cuda_status(launch_clip(job.descs[0], s));
         const int rc2 = finish_staging(job, s);
         return set_last(rc == IWPP_OK ? rc2 : rc);
@@ -790,7 +854,7 @@ int iwpp_sweep(void* marker, const void* mask, size_t pitch_marker, size_t pitch
     Job job;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     iwpp_config c{};
-    rc = build_job(job, &im, 1, IWPP_QUEUE_UNIQUE, &c, s, true);
+    rc = build_job(job, &im, 1, IWPP_QUEUE_UNIQUE, &c, s, STAGE_ASYNC);
     if (rc == IWPP_OK && !job.descs.empty()) rc = cuda_status(launch_sweep(job.descs[0], direction, s));
     const int rc2 = finish_staging(job, s);
     return set_last(rc == IWPP_OK ? rc2 : rc);

@@ -268,3 +268,26 @@ def test_device_wait_timeout_is_reported_not_hung():
     marker0, mask0 = synth.config0()
     out, _ = gpu_reconstruct(marker0, mask0, 8, "unique")
     assert np.array_equal(out, oracle.reconstruct(marker0, mask0, 8))
+
+
+def test_graph_plan_with_unaligned_images():
+    # widths that leave rows unaligned: the plan stages them inside the graph
+    h = iwpp.Handle(0)
+    pairs, refs, pristine = [], [], []
+    for i, (w, hh, dt, conn) in enumerate([(301, 97, 0, 8), (513, 200, 0, 4), (77, 61, 1, 8), (129, 33, 2, 4)]):
+        mask = synth.noise_mask(w, hh, dt, 700 + i, 2.0, 3)
+        marker = synth.hdome_marker(mask, 30)
+        refs.append(oracle.reconstruct(marker, mask, conn))
+        tm, tk = to_dev(marker), to_dev(mask)
+        pristine.append(tm.clone())
+        pairs.append((tm, tk, conn, marker.dtype))
+    plan = iwpp.Plan(h, [(p[0], p[1], p[2]) for p in pairs])
+    for _ in range(2):
+        for p, q in zip(pairs, pristine):
+            p[0].copy_(q)
+        plan.launch()
+        plan.sync()
+        for p, ref in zip(pairs, refs):
+            assert np.array_equal(from_dev(p[0], p[3]), ref)
+    plan.close()
+    h.close()
