@@ -32,9 +32,11 @@ typedef enum iwpp_status {
     IWPP_ERR_CUDA = 4,      /* a CUDA runtime call failed */
     IWPP_ERR_OVERFLOW = 5,  /* queue overflowed more often than max_restarts */
     IWPP_ERR_NO_DEVICE = 6, /* no CUDA device, or not a GB300-class (sm_103) one */
-    IWPP_ERR_BUSY = 7,      /* a server is full or shutting down */
+    IWPP_ERR_BUSY = 7,      /* a server's queue is full or it is shutting down; a
+                               waited-for request is not finished yet */
     IWPP_ERR_TOO_LARGE = 8  /* the image needs more workspace than the static scratch of
-                               iwpp_reconstruct_noalloc holds */
+                               iwpp_reconstruct_noalloc holds, or more device memory
+                               than a server's budget */
 } iwpp_status;
 
 typedef enum iwpp_dtype { IWPP_U8 = 0, IWPP_U16 = 1, IWPP_I32 = 2 } iwpp_dtype;
@@ -124,6 +126,9 @@ IWPP_API int iwpp_handle_sync(iwpp_handle h, iwpp_stats *stats);
 /* ---- batched: all images in one persistent launch ----------------------- */
 IWPP_API int iwpp_reconstruct_batch(iwpp_handle h, const iwpp_image *images, int n, int variant,
                                     const iwpp_config *cfg, void *stream, iwpp_stats *stats);
+/* Same, asynchronous on `stream`; iwpp_handle_sync reports the result. */
+IWPP_API int iwpp_reconstruct_batch_async(iwpp_handle h, const iwpp_image *images, int n, int variant,
+                                          const iwpp_config *cfg, void *stream);
 /* A batch captured once into a CUDA graph (state reset + launches); every
  * iwpp_plan_launch re-runs the reconstruction on the same buffers. */
 IWPP_API int iwpp_plan_create(iwpp_plan *out, iwpp_handle h, const iwpp_image *images, int n, int variant,
@@ -172,6 +177,67 @@ IWPP_API int iwpp_sweep_timing(void *marker, const void *mask, size_t pitch_mark
 #define IWPP_NOALLOC_SCRATCH_BYTES (4u << 20)
 IWPP_API int iwpp_reconstruct_noalloc(void *marker, const void *mask, size_t pitch_marker, size_t pitch_mask,
                                       int width, int height, int dtype, int connectivity, void *stream);
+
+/* ---- serving: a request loop with continuous batching ------------------ */
+/* No counterpart in the reference (its only caller is one main() per image,
+ * IWPP MP/src/main.cu:59).  Requests (host marker / mask / result buffers)
+ * are submitted from any thread and admitted in arrival order while their
+ * device bytes (staging copies of both planes plus queue state) fit the
+ * memory budget.  `lanes` worker threads, each with its own stream and
+ * workspace, take every admitted request that is waiting when they come
+ * free and run them as one batch (one persistent launch), so requests
+ * arriving while others run join the next batch and their copies and
+ * kernels overlap on the device.  Device memory comes from a pool that keeps
+ * what it allocated resident for the life of the server. */
+typedef struct iwpp_server_config {
+    int lanes;                 /* concurrent batches, 0 = 3 */
+    int max_batch;             /* requests per batch, 0 = 256 */
+    int max_pending;           /* waiting requests before submit says BUSY, 0 = 65536 */
+    int variant;               /* queue variant, IWPP_QUEUE_DEFAULT = async */
+    int tile_rows;             /* 0 = default */
+    int lane_ctas;             /* CTAs per batch launch, 0 = the whole GPU */
+    int timeout_ms;            /* device wait bound per batch, 0 = 60000 */
+    long long memory_budget;   /* device bytes for admitted requests, 0 = half the free memory at creation */
+} iwpp_server_config;
+
+typedef struct iwpp_request_result {
+    int status;                /* IWPP_OK or the error of the request's batch */
+    int lane;                  /* lane that ran it */
+    int batch_size;            /* requests in its batch */
+    int reserved;
+    double latency_us;         /* submit -> result in the host buffer */
+    double queue_us;           /* submit -> admitted into a batch */
+    double service_us;         /* admitted -> result in the host buffer */
+} iwpp_request_result;
+
+typedef struct iwpp_server_stats {
+    long long submitted, completed, failed, rejected;
+    long long batches, largest_batch;
+    long long pixels;          /* pixels of completed requests */
+    long long bytes_in_use;    /* device bytes held by admitted requests now */
+    long long bytes_peak;      /* most ever held at once */
+    long long memory_budget;
+} iwpp_server_stats;
+
+typedef struct iwpp_server_s *iwpp_server;
+
+IWPP_API int iwpp_server_create(iwpp_server *out, int device, const iwpp_server_config *cfg);
+/* Enqueues one request; returns at once.  marker and mask are read, out
+ * (out_pitch bytes per row) receives the reconstruction; all three stay
+ * owned by the caller and must stay valid until iwpp_server_wait returns
+ * for the ticket.  Pinned host memory makes the copies asynchronous.
+ * IWPP_ERR_BUSY: max_pending requests are waiting; IWPP_ERR_TOO_LARGE: the
+ * request alone exceeds the memory budget. */
+IWPP_API int iwpp_server_submit(iwpp_server s, const void *marker, const void *mask, void *out, size_t pitch_marker,
+                                size_t pitch_mask, size_t pitch_out, int width, int height, int dtype,
+                                int connectivity, unsigned long long *ticket);
+/* Waits up to timeout_ms (< 0: forever) for a ticket; IWPP_ERR_BUSY if it
+ * is not finished by then.  On completion returns the request's status,
+ * fills `result` (nullable) and forgets the ticket. */
+IWPP_API int iwpp_server_wait(iwpp_server s, unsigned long long ticket, int timeout_ms, iwpp_request_result *result);
+IWPP_API int iwpp_server_stats_get(iwpp_server s, iwpp_server_stats *stats);
+/* Finishes every submitted request, then stops the lanes and frees the pool. */
+IWPP_API int iwpp_server_destroy(iwpp_server s);
 
 /* ---- reference-compatible entry points --------------------------------- */
 /* Exactly the reference signature (IWPP MP/include/MorphologicalReconstruction.cuh:45-46;

@@ -550,6 +550,20 @@ int run_job_sync(iwpp_handle h, const iwpp_image* imgs, int n, int variant, cons
 
 }  // namespace
 
+namespace iwpp {
+// Grows a handle's workspace ahead of use (the server sizes each lane once).
+int handle_reserve(iwpp_handle h, size_t bytes) {
+    if (!h) return IWPP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(h->mu);
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (prev != h->device) cudaSetDevice(h->device);
+    const int rc = ensure_workspace(h->ws, bytes);
+    if (prev != h->device) cudaSetDevice(prev);
+    return rc;
+}
+}  // namespace iwpp
+
 // ====================================================================== API
 extern "C" {
 
@@ -562,8 +576,8 @@ const char* iwpp_status_string(int status) {
         case IWPP_ERR_CUDA: return "CUDA runtime error";
         case IWPP_ERR_OVERFLOW: return "queue overflow restarts exhausted";
         case IWPP_ERR_NO_DEVICE: return "no sm_103 (GB300) CUDA device";
-        case IWPP_ERR_BUSY: return "server full or shutting down";
-        case IWPP_ERR_TOO_LARGE: return "image too large for the no-allocation scratch";
+        case IWPP_ERR_BUSY: return "server queue full, shutting down, or request not finished";
+        case IWPP_ERR_TOO_LARGE: return "image too large for the no-allocation scratch or the server budget";
         default: return "unknown status";
     }
 }
@@ -633,29 +647,40 @@ int iwpp_reconstruct_batch(iwpp_handle h, const iwpp_image* images, int n, int v
     return set_last(run_job_sync(h, images, n, variant, cfg, static_cast<cudaStream_t>(stream), stats));
 }
 
-int iwpp_reconstruct_async(iwpp_handle h, void* marker, const void* mask, size_t pitch_marker, size_t pitch_mask,
-                           int width, int height, int dtype, int connectivity, int variant, const iwpp_config* cfg,
-                           void* stream) {
-    if (!h) return set_last(IWPP_ERR_INVALID);
+int iwpp_reconstruct_batch_async(iwpp_handle h, const iwpp_image* images, int n, int variant, const iwpp_config* cfg,
+                                 void* stream) {
+    if (!h || n < 0 || (n > 0 && !images)) return set_last(IWPP_ERR_INVALID);
     std::lock_guard<std::mutex> lk(h->mu);
+    int prev_dev = 0;
+    cudaGetDevice(&prev_dev);
+    if (prev_dev != h->device) cudaSetDevice(h->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    iwpp_image im{marker, mask, pitch_marker, pitch_mask, width, height, dtype, connectivity};
     Job job;
-    int rc = build_job(job, &im, 1, variant, cfg, s, STAGE_ASYNC);
+    int rc = build_job(job, images, n, variant, cfg, s, STAGE_ASYNC);
     if (rc == IWPP_OK) rc = enqueue_job(job, h->ws, s, h->device, true, h->ev0, h->ev1, true);
     const int rc2 = finish_staging(job, s);
     if (rc == IWPP_OK) rc = rc2;
-    if (rc == IWPP_OK) {
+    if (rc == IWPP_OK && h->ws.base) {
         // queue the counters copy behind the job; iwpp_handle_sync waits for it
         cudaError_t e = cudaMemcpyAsync(h->host_ctrl, h->ws.base, sizeof(Ctrl), cudaMemcpyDeviceToHost, s);
         rc = cuda_status(e);
+    } else if (rc == IWPP_OK) {
+        std::memset(h->host_ctrl, 0, sizeof(Ctrl));
     }
     h->last_stream = s;
     h->last_tiles = job.G;
     h->last_variant = job.variant;
     h->last_launch_status = rc;
-    h->timed = true;
+    h->timed = job.G > 0;
+    if (prev_dev != h->device) cudaSetDevice(prev_dev);
     return set_last(rc);
+}
+
+int iwpp_reconstruct_async(iwpp_handle h, void* marker, const void* mask, size_t pitch_marker, size_t pitch_mask,
+                           int width, int height, int dtype, int connectivity, int variant, const iwpp_config* cfg,
+                           void* stream) {
+    iwpp_image im{marker, mask, pitch_marker, pitch_mask, width, height, dtype, connectivity};
+    return iwpp_reconstruct_batch_async(h, &im, 1, variant, cfg, stream);
 }
 
 int iwpp_handle_sync(iwpp_handle h, iwpp_stats* stats) {

@@ -28,7 +28,8 @@ VARIANTS = {"mutex": MUTEX, "mp": MUTEX, "double": DOUBLE, "dq": DOUBLE, "unique
             "async": ASYNC, "default": DEFAULT}
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "timeout", 4: "CUDA error",
-          5: "queue overflow restarts exhausted", 6: "no sm_103 device", 7: "busy", 8: "too large for the scratch"}
+          5: "queue overflow restarts exhausted", 6: "no sm_103 device", 7: "busy / not finished",
+          8: "too large for the scratch or the server budget"}
 
 
 class IwppError(RuntimeError):
@@ -69,6 +70,30 @@ class Image(ctypes.Structure):
                 ("dtype", ctypes.c_int), ("connectivity", ctypes.c_int)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("lanes", ctypes.c_int), ("max_batch", ctypes.c_int), ("max_pending", ctypes.c_int),
+                ("variant", ctypes.c_int), ("tile_rows", ctypes.c_int), ("lane_ctas", ctypes.c_int),
+                ("timeout_ms", ctypes.c_int), ("memory_budget", ctypes.c_longlong)]
+
+
+class RequestResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("lane", ctypes.c_int), ("batch_size", ctypes.c_int),
+                ("reserved", ctypes.c_int), ("latency_us", ctypes.c_double), ("queue_us", ctypes.c_double),
+                ("service_us", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_longlong) for k in ("submitted", "completed", "failed", "rejected", "batches",
+                                                 "largest_batch", "pixels", "bytes_in_use", "bytes_peak",
+                                                 "memory_budget")]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # Every symbol include/iwpp.h declares, with its ctypes signature.
 _SIGS = {
     "iwpp_status_string": (ctypes.c_char_p, [ctypes.c_int]),
@@ -88,6 +113,8 @@ _SIGS = {
     "iwpp_handle_sync": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)]),
     "iwpp_reconstruct_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Image), ctypes.c_int, ctypes.c_int,
                                               ctypes.POINTER(Config), ctypes.c_void_p, ctypes.POINTER(Stats)]),
+    "iwpp_reconstruct_batch_async": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Image), ctypes.c_int,
+                                                    ctypes.c_int, ctypes.POINTER(Config), ctypes.c_void_p]),
     "iwpp_plan_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_void_p, ctypes.POINTER(Image),
                                         ctypes.c_int, ctypes.c_int, ctypes.POINTER(Config)]),
     "iwpp_plan_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
@@ -103,6 +130,16 @@ _SIGS = {
     "iwpp_reconstruct_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
                                                 ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_void_p]),
+    "iwpp_server_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                                          ctypes.POINTER(ServerConfig)]),
+    "iwpp_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.POINTER(ctypes.c_ulonglong)]),
+    "iwpp_server_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_int,
+                                        ctypes.POINTER(RequestResult)]),
+    "iwpp_server_stats_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ServerStats)]),
+    "iwpp_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "MorphologicalReconstruction": (None, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
                                            ctypes.c_int]),
     "configureHeapSize": (None, []),
@@ -352,3 +389,85 @@ def sweep_timing(marker, mask, connectivity: int = 8) -> list[float]:
 
 def tile_count(width: int, height: int, dtype: int, tile_rows: int = 0) -> int:
     return int(load().iwpp_tile_count(width, height, dtype, tile_rows))
+
+
+_NP_DTYPES = {"uint8": U8, "uint16": U16, "int32": I32}
+
+
+class Server:
+    """The serving loop (``iwpp_server_*``): host numpy requests admitted by
+    a device-memory budget and run in continuous batches over ``lanes``
+    streams.  ``submit`` returns a ticket at once; ``wait`` returns the
+    reconstruction (a new array, or ``out``) and the request's timings."""
+
+    def __init__(self, device: int = 0, lanes: int = 0, max_batch: int = 0, max_pending: int = 0,
+                 variant="default", tile_rows: int = 0, lane_ctas: int = 0, timeout_ms: int = 0,
+                 memory_budget: int = 0):
+        lib = load()
+        cfg = ServerConfig(lanes, max_batch, max_pending, _variant(variant), tile_rows, lane_ctas, timeout_ms,
+                           memory_budget)
+        p = ctypes.c_void_p()
+        st = lib.iwpp_server_create(ctypes.byref(p), device, ctypes.byref(cfg))
+        if st != 0:
+            raise IwppError(st, "iwpp_server_create")
+        self._p = p
+        self._held = {}
+
+    def submit(self, marker, mask, connectivity: int = 8, out=None) -> int:
+        import numpy as np
+        if marker.shape != mask.shape or marker.dtype != mask.dtype or marker.ndim != 2:
+            raise ValueError("marker and mask must be 2-D arrays of one shape and dtype")
+        code = _NP_DTYPES.get(str(marker.dtype))
+        if code is None:
+            raise TypeError(f"unsupported dtype {marker.dtype}")
+        if out is None:
+            out = np.empty_like(marker)
+        if out.shape != marker.shape or out.dtype != marker.dtype:
+            raise ValueError("out must match marker")
+        for a in (marker, mask, out):
+            if a.strides[1] != a.itemsize:
+                raise ValueError("rows must be contiguous")
+        h, w = marker.shape
+        t = ctypes.c_ulonglong()
+        st = load().iwpp_server_submit(self._p, marker.ctypes.data, mask.ctypes.data, out.ctypes.data,
+                                       marker.strides[0], mask.strides[0], out.strides[0], w, h, code,
+                                       connectivity, ctypes.byref(t))
+        if st != 0:
+            raise IwppError(st, "iwpp_server_submit")
+        self._held[t.value] = (marker, mask, out)
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        r = RequestResult()
+        st = load().iwpp_server_wait(self._p, ticket, timeout_ms, ctypes.byref(r))
+        if st == 7:
+            raise TimeoutError(f"request {ticket} not finished")
+        held = self._held.pop(ticket, None)
+        if st != 0:
+            raise IwppError(st, "iwpp_server_wait")
+        return held[2], r.as_dict()
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        st = load().iwpp_server_stats_get(self._p, ctypes.byref(s))
+        if st != 0:
+            raise IwppError(st, "iwpp_server_stats_get")
+        return s.as_dict()
+
+    def close(self):
+        if getattr(self, "_p", None):
+            load().iwpp_server_destroy(self._p)
+            self._p = None
+            self._held.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -95,3 +95,25 @@ def test_no_device_reported_without_gpu():
     # a valid empty image needs no device at all
     st = iwpp.Stats()
     assert lib.iwpp_reconstruct(None, None, None, 0, 0, 0, 0, 0, 8, 2, None, None, ctypes.byref(st)) == 0
+
+
+def test_server_host_side_checks():
+    lib = iwpp.load()
+    srv = ctypes.c_void_p()
+    bad = iwpp.ServerConfig(lanes=-1)
+    assert lib.iwpp_server_create(ctypes.byref(srv), 0, ctypes.byref(bad)) == 1
+    bad = iwpp.ServerConfig(tile_rows=48)
+    assert lib.iwpp_server_create(ctypes.byref(srv), 0, ctypes.byref(bad)) == 1
+    assert lib.iwpp_server_create(None, 0, None) == 1
+    t = ctypes.c_ulonglong()
+    assert lib.iwpp_server_submit(None, 16, 16, 16, 64, 64, 64, 64, 64, 0, 8, ctypes.byref(t)) == 1
+    assert lib.iwpp_server_wait(None, 1, 0, None) == 1
+    assert lib.iwpp_server_stats_get(None, None) == 1
+    assert lib.iwpp_server_destroy(None) == 0
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return
+    except ImportError:
+        pass
+    assert lib.iwpp_server_create(ctypes.byref(srv), 0, None) == 6
