@@ -4,8 +4,9 @@
 Workload (one "step"): the six plain 4096x4096 uint8 reconstructions of the
 4096^2 configuration -- connectivity {4, 8} x h-dome h {10, 40, 100} on one
 seeded smoothed-noise-plus-discs mask -- each through the C ABI with the
-unique queue.  Every reconstruction restores its marker from a pristine
-device copy first (in place).
+async queue (--variant picks mutex / double / unique).  Every
+reconstruction restores its marker from a pristine device copy first (in
+place).
 
   value : device-resident throughput (inputs already in HBM), CUDA events
           around K steps on the launching stream, max over ranks.
@@ -18,6 +19,15 @@ device copy first (in place).
           measured HBM copy bandwidth.
   cpu_baseline : the CPU oracle (Vincent 1993 hybrid, single thread) on the
           same six images, also used to check the GPU output bit for bit.
+
+Sub-results in the same line (skipped with --no-extras):
+  batched : 64 uneven images in one CUDA-graph plan vs 64 sequential plain
+          calls, Gpixels/s of each, bit-exact against each other and the
+          oracle.
+  served : a 2000 req/s Poisson stream through the serving loop (open loop:
+          p50 / p99 latency; closed loop: saturated Gpixels/s) vs plain
+          per-request calls, with host buffers, every result bit-exact.
+  spiral : the 16384^2 spiral-corridor worst case in uint8 / uint16 / int32.
 
 --impl reference times the reference's CPU path for the same workload.  The
 reference has no CPU implementation, so that is the oracle port, one host
@@ -46,7 +56,7 @@ for p in (os.path.join(REPO, "iwpp-mp_gb300"), REPO):
 METRIC = "Gpixels/s bit-exact reconstruction (plain vs batched); served p50/p99 latency"
 UNIT = "Gpixels/s"
 WORKLOAD = ("4096x4096 uint8 plain reconstruction, seed 1, sigma 8, 2000 discs, h-dome h in {10,40,100} x "
-            "connectivity {4,8} (6 images per step), unique queue")
+            "connectivity {4,8} (6 images per step)")
 
 
 def _dist_env():
@@ -182,6 +192,226 @@ def run_reference(args):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def _to_dev(a, dev):
+    import numpy as np
+    import torch
+
+    return torch.from_numpy(a.view(np.int16) if a.dtype == np.uint16 else a).to(dev)
+
+
+def _from_dev(t, dtype):
+    import numpy as np
+
+    a = t.cpu().numpy()
+    return a.view(np.uint16) if dtype == np.uint16 else a
+
+
+def _pinned(a):
+    """A page-locked copy of a numpy array (through torch), same dtype."""
+    import numpy as np
+    import torch
+
+    t = torch.from_numpy(a.view(np.int16) if a.dtype == np.uint16 else a).pin_memory()
+    n = t.numpy()
+    return n.view(np.uint16) if a.dtype == np.uint16 else n
+
+
+def bench_batched(args, dev, variant):
+    """64 images of uneven sizes (uint8 / uint16, 4/8-connectivity, h-dome
+    h in [5, 120], seed 3): one CUDA-graph plan (one persistent launch over
+    all tiles) against 64 sequential plain synchronous calls on the same
+    device-resident inputs."""
+    import numpy as np
+    import torch
+
+    import iwpp
+    from iwpp import synth
+
+    specs = synth.config3_specs(64)
+    imgs = [synth.spec_images(s, nthreads=os.cpu_count() or 1) for s in specs]
+    px = sum(s.pixels for s in specs)
+    nbytes = sum(3 * s.pixels * s.bpp for s in specs)
+    h = iwpp.Handle(dev.index or 0)
+    pm = [_to_dev(m, dev) for m, _ in imgs]
+    pk = [_to_dev(k, dev) for _, k in imgs]
+    work = [p.clone() for p in pm]
+    reps = max(args.warmup, 3) + 5
+
+    def restore():
+        for w, p in zip(work, pm):
+            w.copy_(p)
+        torch.cuda.synchronize()
+
+    seq = []
+    for _ in range(reps):
+        restore()
+        t = time.perf_counter()
+        for w, k, s in zip(work, pk, specs):
+            iwpp.reconstruct(w, k, connectivity=s.conn, variant=variant, handle=h)
+        seq.append(time.perf_counter() - t)
+    seq_out = [_from_dev(w, m.dtype) for w, (m, _) in zip(work, imgs)]
+    plan = iwpp.Plan(h, [(w, k, s.conn) for w, k, s in zip(work, pk, specs)], variant=variant)
+    graph = []
+    for _ in range(reps):
+        restore()
+        t = time.perf_counter()
+        plan.launch()
+        st = plan.sync()
+        graph.append(time.perf_counter() - t)
+    plan_ok = all(np.array_equal(_from_dev(w, m.dtype), ref) for w, (m, _), ref in zip(work, imgs, seq_out))
+    oracle_ok = None
+    if not args.no_cpu:
+        import oracle
+        from concurrent.futures import ThreadPoolExecutor
+
+        with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+            refs = list(ex.map(lambda i: oracle.reconstruct(imgs[i][0], imgs[i][1], specs[i].conn),
+                               range(len(specs))))
+        oracle_ok = all(np.array_equal(a, b) for a, b in zip(seq_out, refs))
+    plan.close()
+    h.close()
+    t_seq = statistics.median(seq[max(args.warmup, 3):])
+    t_plan = statistics.median(graph[max(args.warmup, 3):])
+    return {"workload": f"64 images, sizes log-uniform 512..4096 x 512..3072 (seed 3, {px / 1e6:.1f} Mpx), "
+                        "uint8/uint16, 4/8-conn, h-dome h in [5,120]; device-resident",
+            "plan_gpx_s": px / t_plan / 1e9, "sequential_gpx_s": px / t_seq / 1e9, "speedup": t_seq / t_plan,
+            "plan_ms": t_plan * 1e3, "sequential_ms": t_seq * 1e3,
+            "plan_hbm_frac": nbytes / t_plan / 1e9 / peak_hbm()[0], "tiles": st.tiles, "visits": st.visits,
+            "bitexact_plan_vs_sequential": plan_ok, "bitexact_vs_oracle": oracle_ok,
+            "timing": f"median of {reps - max(args.warmup, 3)} after {max(args.warmup, 3)} warm-up, host clock "
+                      "around launch + sync, markers restored before each"}
+
+
+def bench_served(args, dev, variant):
+    """Poisson request stream (2000 req/s, seed 4) of 8-connected uint8 (80 %)
+    / uint16 images, sides log-uniform 256..8192, h-dome or sparse-seed
+    markers, through the serving loop (iwpp_server_*) with pinned host
+    buffers; against plain per-request synchronous calls (H2D, reconstruct,
+    D2H) on the same requests."""
+    import numpy as np
+    import torch
+
+    import iwpp
+    from iwpp import synth
+
+    n_req = args.served_requests
+    times, which, specs = synth.config4_stream(n_req, 48)
+    imgs = [synth.spec_images(s, nthreads=os.cpu_count() or 1) for s in specs]
+    pin = [(_pinned(m), _pinned(k)) for m, k in imgs]
+    outs = [_pinned(np.zeros_like(m)) for m, _ in imgs]
+    px = sum(specs[w].pixels for w in which)
+    h = iwpp.Handle(dev.index or 0)
+    refs = []
+    for (m, k), s in zip(pin, specs):  # one plain call per distinct image
+        dm, dk = _to_dev(m, dev), _to_dev(k, dev)
+        iwpp.reconstruct(dm, dk, connectivity=8, variant=variant, handle=h)
+        refs.append(_from_dev(dm, m.dtype))
+    oracle_ok = None
+    if not args.no_cpu:
+        import oracle
+        from concurrent.futures import ThreadPoolExecutor
+
+        with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+            orefs = list(ex.map(lambda i: oracle.reconstruct(imgs[i][0], imgs[i][1], 8), range(len(specs))))
+        oracle_ok = all(np.array_equal(a, b) for a, b in zip(refs, orefs))
+
+    # plain per-request calls, closed loop, same pinned host buffers
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for w in which:
+        m, k = pin[w]
+        dm, dk = _to_dev(m, dev), _to_dev(k, dev)
+        iwpp.reconstruct(dm, dk, connectivity=8, variant=variant, handle=h)
+        o = outs[w]
+        torch.from_numpy(o.view(np.int16) if o.dtype == np.uint16 else o).copy_(dm)
+    t_plain = time.perf_counter() - t
+    plain_ok = all(np.array_equal(outs[w], refs[w]) for w in set(which))
+    h.close()
+
+    def run(open_loop):
+        for o in outs:
+            o.fill(0)
+        with iwpp.Server(device=dev.index or 0, lanes=args.lanes, variant=variant) as srv:
+            for w in range(len(specs)):  # warm the pool and the lanes
+                srv.wait(srv.submit(pin[w][0], pin[w][1], 8, out=outs[w]))
+            tickets = []
+            t0 = time.perf_counter()
+            for i, w in enumerate(which):
+                if open_loop:
+                    while time.perf_counter() - t0 < times[i]:
+                        pass
+                tickets.append(srv.submit(pin[w][0], pin[w][1], 8, out=outs[w]))
+            lat, status_ok = [], True
+            for tk in tickets:
+                _, info = srv.wait(tk)
+                lat.append(info["latency_us"] / 1e3)
+                status_ok &= info["status"] == 0
+            dt = time.perf_counter() - t0
+            st = srv.stats()
+        ok = status_ok and all(np.array_equal(outs[w], refs[w]) for w in set(which))
+        lat = np.array(lat)
+        return {"gpx_s": px / dt / 1e9, "seconds": dt, "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "batches": st["batches"],
+                "largest_batch": st["largest_batch"], "device_bytes_peak": st["bytes_peak"], "bitexact": ok}
+
+    served = run(True)
+    saturated = run(False)
+    return {"workload": f"{n_req} requests, Poisson 2000/s (seed 4), sides log-uniform 256..8192 "
+                        f"({px / n_req / 1e6:.2f} Mpx mean), uint8 80% / uint16 20%, 8-conn, "
+                        "h-dome or 0.01% sparse seeds; pinned host buffers, H2D + D2H included",
+            "offered_gpx_s": px / times[-1] / 1e9, "lanes": args.lanes,
+            "open_loop": served, "closed_loop": saturated,
+            "plain_per_request_gpx_s": px / t_plain / 1e9, "plain_bitexact": plain_ok,
+            "speedup_vs_plain": saturated["gpx_s"] / (px / t_plain / 1e9),
+            "bitexact_vs_oracle": oracle_ok}
+
+
+def bench_spiral(args, dev, variant):
+    """16384 x 16384 spiral-corridor worst case (seed 2, sigma 16, arm pitch
+    256, 64 seeds), uint8 / uint16 / int32, 8-connectivity."""
+    import numpy as np
+    import torch
+
+    import iwpp
+    from iwpp import synth
+
+    res = {}
+    h = iwpp.Handle(dev.index or 0)
+    peak = peak_hbm()[0]
+    for name, dt in (("u8", synth.U8), ("u16", synth.U16), ("i32", synth.I32)):
+        marker, mask, _ = synth.config2(dt)
+        H, W = mask.shape
+        bpp = mask.dtype.itemsize
+        m0, k = _to_dev(marker, dev), _to_dev(mask, dev)
+        m = m0.clone()
+        times = []
+        for rep in range(1 + args.spiral_reps):
+            m.copy_(m0)
+            torch.cuda.synchronize()
+            st = iwpp.reconstruct(m, k, connectivity=8, variant=variant, handle=h)
+            if rep:
+                times.append(st.device_ms)
+        t = statistics.median(times) / 1e3
+        entry = {"ms": t * 1e3, "gpx_s": W * H / t / 1e9, "hbm_frac": 3 * W * H * bpp / t / 1e9 / peak,
+                 "visits": st.visits, "tiles": st.tiles}
+        if name == "u8" and not args.no_cpu:
+            import oracle
+
+            t0 = time.perf_counter()
+            ref = oracle.reconstruct(marker, mask, 8)
+            entry["cpu_oracle_s"] = time.perf_counter() - t0
+            entry["bitexact_vs_oracle"] = bool(np.array_equal(_from_dev(m, marker.dtype), ref))
+            del ref
+        res[name] = entry
+        del m, m0, k
+        torch.cuda.empty_cache()
+    h.close()
+    res["workload"] = ("16384x16384, 8-conn, smoothed noise (seed 2, sigma 16) with a 1-px spiral corridor "
+                       "(arm pitch 256) at the dtype maximum, marker 0 but 64 seeds; device time per "
+                       f"reconstruction, median of {args.spiral_reps}")
+    return res
 
 
 def run_ours(args):
@@ -322,8 +552,14 @@ def run_ours(args):
         "clocks": clock_info,
         "gpu_launches": args.steps * len(cases) * 2,
     }
-    print(json.dumps(line), flush=True)
     handle.close()
+    if not args.no_extras:
+        for key, fn in (("batched", bench_batched), ("served", bench_served), ("spiral", bench_spiral)):
+            try:
+                line[key] = fn(args, dev, variant)
+            except Exception as exc:  # reported in the line, the headline stands
+                line[key] = {"error": f"{type(exc).__name__}: {exc}"}
+    print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
@@ -332,12 +568,17 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--variant", default="unique", choices=["mutex", "double", "unique"])
+    ap.add_argument("--variant", default="async", choices=["mutex", "double", "unique", "async"])
     ap.add_argument("--tile-rows", type=int, default=0)
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline / bit-exact check")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline / bit-exact checks")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="only the headline line (no batched / served / spiral sub-results)")
+    ap.add_argument("--served-requests", type=int, default=4000)
+    ap.add_argument("--lanes", type=int, default=3)
+    ap.add_argument("--spiral-reps", type=int, default=3)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

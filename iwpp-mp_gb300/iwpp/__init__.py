@@ -425,12 +425,13 @@ class Server:
         if out.shape != marker.shape or out.dtype != marker.dtype:
             raise ValueError("out must match marker")
         for a in (marker, mask, out):
-            if a.strides[1] != a.itemsize:
+            if a.size and a.strides[1] != a.itemsize:
                 raise ValueError("rows must be contiguous")
         h, w = marker.shape
         t = ctypes.c_ulonglong()
+        pitches = [a.strides[0] if a.size else w * a.itemsize for a in (marker, mask, out)]
         st = load().iwpp_server_submit(self._p, marker.ctypes.data, mask.ctypes.data, out.ctypes.data,
-                                       marker.strides[0], mask.strides[0], out.strides[0], w, h, code,
+                                       pitches[0], pitches[1], pitches[2], w, h, code,
                                        connectivity, ctypes.byref(t))
         if st != 0:
             raise IwppError(st, "iwpp_server_submit")
