@@ -62,6 +62,9 @@ typedef struct iwpp_config {
     int clip_marker;           /* 1: marker = min(marker, mask) before reconstructing */
     int plain_loads;           /* 1: never use TMA box loads (else TMA whenever base and
                                   pitch are 16-byte aligned) */
+    int solver;                /* in-tile solver: 0 = automatic, 1 = row sweeps (fewest
+                                  instructions), 2 = vertical / horizontal passes
+                                  (shortest latency) */
 } iwpp_config;
 
 typedef struct iwpp_stats {

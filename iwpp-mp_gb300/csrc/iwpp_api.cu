@@ -60,6 +60,7 @@ struct Config {
     int timeout_ms;
     int clip_marker;
     int plain_loads;
+    int solver;
 };
 
 Config resolve_config(const iwpp_config* c) {
@@ -72,6 +73,7 @@ Config resolve_config(const iwpp_config* c) {
     r.timeout_ms = c && c->timeout_ms > 0 ? c->timeout_ms : 10000;
     r.clip_marker = c ? c->clip_marker : 0;
     r.plain_loads = c ? c->plain_loads : 0;
+    r.solver = c && c->solver >= 0 && c->solver <= 2 ? c->solver : 0;
     if (std::getenv("IWPP_PLAIN_LOADS")) r.plain_loads = 1;
     return r;
 }
@@ -410,6 +412,7 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
     a.ctrl = reinterpret_cast<Ctrl*>(base);
     a.timeout_ns = (long long)job.cfg.timeout_ms * 1000000ll;
     a.max_restarts = job.cfg.max_restarts;
+    a.solver = job.cfg.solver;
 
     cudaError_t e = cudaSuccess;
     if (upload_descs && !job.descs.empty()) {

@@ -327,6 +327,196 @@ __device__ __forceinline__ void sweep(WarpSmem<TH>& sm, int lane, unsigned long 
     __syncwarp();
 }
 
+// ------------------------------------------------------- in-tile passes
+// The tile converges through three kinds of pass, the separable form of the
+// reference's XForward / XBackward / YDownward / YUpward propagation
+// (MR.cu:34-161):
+//   vertical down / up: each lane walks its own columns over the rows, one
+//     row per step, taking the row before it (8-connectivity: its three
+//     upper / lower neighbours, the outer two through one shuffle each);
+//     no vote or scan per row, so a row costs a few dependent operations;
+//   horizontal: rows are independent, each gets a forward and a backward
+//     max-min scan across the warp (hscan); four rows are scanned together
+//     so their shuffle latencies overlap.
+// Rows are numbered as in shared memory (1..TH); masks use bit r-1.
+
+// OR of a per-lane 64-bit mask over the warp.
+__device__ __forceinline__ unsigned long long warp_or64(unsigned long long v) {
+    const unsigned lo = __reduce_or_sync(FULL, (unsigned)v);
+    const unsigned hi = __reduce_or_sync(FULL, (unsigned)(v >> 32));
+    return ((unsigned long long)hi << 32) | lo;
+}
+
+// Vertical pass, downward (rows in increasing order) or upward, from the
+// first row of `dirty` (rows whose constraint towards the row before them,
+// in pass order, may be violated) to the tile's far edge.  It does not stop
+// where the rows stop rising: a vote there costs more latency on long
+// fronts than the rows it would save.  Returns the rows that rose
+// (warp-uniform); `col_now` (per lane) records a rise in the tile's first /
+// last pixel column; `steps` counts the rows processed.
+template <int DT, int CONN, int TH, bool DOWN>
+__device__ __forceinline__ unsigned long long vpass(WarpSmem<TH>& sm, int lane, unsigned long long dirty,
+                                                    uint32_t edge_mask, bool& col_now, unsigned& steps) {
+    using P = Px<DT>;
+    constexpr int N = P::PPW;
+    const int first = DOWN ? __ffsll((long long)dirty) : 64 - __clzll((long long)dirty);
+    uint32_t prev[N];
+    P::unpack(sm.tm[(DOWN ? first - 1 : first + 1) * 32 + lane], prev);
+    const int count = DOWN ? TH - first + 1 : first;
+    steps += (unsigned)count;
+    unsigned long long chg = 0ull;
+    uint32_t diff = 0u;
+#pragma unroll 4
+    for (int i = 0; i < count; ++i) {
+        const int r = DOWN ? first + i : first - i;
+        const int rp = DOWN ? r - 1 : r + 1;
+        const uint32_t old = sm.tm[r * 32 + lane];
+        uint32_t m[N], k[N];
+        P::unpack(old, m);
+        P::unpack(sm.tk[r * 32 + lane], k);
+        if (CONN == 8) {
+            uint32_t left = __shfl_up_sync(FULL, prev[N - 1], 1);
+            uint32_t right = __shfl_down_sync(FULL, prev[0], 1);
+            if (lane == 0) left = sm.hLm[rp];
+            if (lane == 31) right = sm.hRm[rp];
+            if (N == 1) {
+                m[0] = P::mx(m[0], P::mn(P::mx3(left, prev[0], right), k[0]));
+            } else {
+#pragma unroll
+                for (int j = 0; j < N; ++j) {
+                    const uint32_t a = j == 0 ? left : prev[j - 1];
+                    const uint32_t c = j == N - 1 ? right : prev[j + 1];
+                    m[j] = P::mx(m[j], P::mn(P::mx3(a, prev[j], c), k[j]));
+                }
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < N; ++j) m[j] = P::mx(m[j], P::mn(prev[j], k[j]));
+        }
+        const uint32_t nw = P::pack(m);
+        sm.tm[r * 32 + lane] = nw;
+        const uint32_t x = nw ^ old;
+        diff |= x;
+        if (x != 0u) chg |= 1ull << (r - 1);
+#pragma unroll
+        for (int j = 0; j < N; ++j) prev[j] = m[j];
+    }
+    col_now |= (diff & edge_mask) != 0u;
+    __syncwarp();
+    return warp_or64(chg);
+}
+
+// R independent rows scanned together in one direction (see hscan).
+template <int DT, bool FWD, int R>
+__device__ __forceinline__ void hscan_rows(uint32_t (&m)[R][Px<DT>::PPW], const uint32_t (&k)[R][Px<DT>::PPW],
+                                           const uint32_t (&cin)[R], int lane) {
+    using P = Px<DT>;
+    constexpr int N = P::PPW;
+    const int first = FWD ? 0 : N - 1, last = FWD ? N - 1 : 0;
+    const int edge_lane = FWD ? 0 : 31;
+    bool need = false;
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+#pragma unroll
+        for (int s = 1; s < N; ++s) {
+            const int j = FWD ? s : N - 1 - s;
+            const int jp = FWD ? j - 1 : j + 1;
+            m[q][j] = P::mx(m[q][j], P::mn(m[q][jp], k[q][j]));
+        }
+        uint32_t in_px = FWD ? __shfl_up_sync(FULL, m[q][last], 1) : __shfl_down_sync(FULL, m[q][last], 1);
+        if (lane == edge_lane) in_px = cin[q];
+        need |= P::gt(P::mn(in_px, k[q][first]), m[q][first]);
+    }
+    // A carry that does not raise a word's entry pixel raises nothing after
+    // it; rows that need no scan come out of it unchanged.
+    if (!__any_sync(FULL, need)) return;
+    uint32_t A[R], B[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        A[q] = m[q][last];
+        B[q] = k[q][0];
+#pragma unroll
+        for (int j = 1; j < N; ++j) B[q] = P::mn(B[q], k[q][j]);
+        if (lane == edge_lane) {
+            A[q] = P::mx(A[q], P::mn(cin[q], B[q]));
+            B[q] = P::MINPX;  // the entry lane becomes a constant: nothing before it
+        }
+    }
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const bool valid = FWD ? (lane >= d) : (lane + d < 32);
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            uint32_t Ap, Bp;
+            if (DT == DT_I32) {
+                Ap = FWD ? __shfl_up_sync(FULL, A[q], d) : __shfl_down_sync(FULL, A[q], d);
+                Bp = FWD ? __shfl_up_sync(FULL, B[q], d) : __shfl_down_sync(FULL, B[q], d);
+            } else {
+                uint32_t pk = A[q] | (B[q] << 16);
+                pk = FWD ? __shfl_up_sync(FULL, pk, d) : __shfl_down_sync(FULL, pk, d);
+                Ap = pk & 0xffffu;
+                Bp = pk >> 16;
+            }
+            if (valid) {
+                A[q] = P::mx(P::mn(Ap, B[q]), A[q]);
+                B[q] = P::mn(Bp, B[q]);
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        uint32_t c = FWD ? __shfl_up_sync(FULL, A[q], 1) : __shfl_down_sync(FULL, A[q], 1);
+        if (lane == edge_lane) c = cin[q];
+#pragma unroll
+        for (int s = 0; s < N; ++s) {
+            const int j = FWD ? s : N - 1 - s;
+            c = P::mn(c, k[q][j]);
+            m[q][j] = P::mx(m[q][j], c);
+        }
+    }
+}
+
+// Horizontal pass over the rows in `rows` (in blocks of four): forward then
+// backward scan, which leaves each row at its one-dimensional fixed point.
+template <int DT, int TH>
+__device__ __forceinline__ unsigned long long hpass(WarpSmem<TH>& sm, int lane, unsigned long long rows,
+                                                    uint32_t edge_mask, bool& col_now, unsigned& blocks) {
+    using P = Px<DT>;
+    constexpr int N = P::PPW;
+    constexpr int R = 4;
+    unsigned long long chg = 0ull;
+    uint32_t diff = 0u;
+#pragma unroll 1
+    for (int b = 0; b < TH; b += R) {
+        if (((rows >> b) & ((1ull << R) - 1ull)) == 0ull) continue;
+        ++blocks;
+        uint32_t m[R][N], k[R][N], old[R], cin[R];
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            const int r = b + q + 1;
+            old[q] = sm.tm[r * 32 + lane];
+            P::unpack(old[q], m[q]);
+            P::unpack(sm.tk[r * 32 + lane], k[q]);
+            cin[q] = sm.hLm[r];
+        }
+        hscan_rows<DT, true, R>(m, k, cin, lane);
+#pragma unroll
+        for (int q = 0; q < R; ++q) cin[q] = sm.hRm[b + q + 1];
+        hscan_rows<DT, false, R>(m, k, cin, lane);
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            const uint32_t nw = P::pack(m[q]);
+            sm.tm[(b + q + 1) * 32 + lane] = nw;
+            const uint32_t x = nw ^ old[q];
+            diff |= x;
+            if (x != 0u) chg |= 1ull << (b + q);
+        }
+    }
+    col_now |= (diff & edge_mask) != 0u;
+    __syncwarp();
+    return warp_or64(chg);
+}
+
 // --------------------------------------------------------------- tile visit
 struct VisitResult {
     unsigned nb;         // NB_* bits: neighbours to notify
@@ -349,6 +539,120 @@ __device__ __forceinline__ uint32_t load_word_plain(const unsigned char* row, in
     return P::pack(p);
 }
 
+// Stores the rows of `rows` (bit r for tile row r) from shared memory to the
+// tile's own pixels (MR.cu:335-364; here plain stores: the visiting warp owns
+// the tile).
+template <int DT, int TH>
+__device__ __forceinline__ void write_back_rows(const ImgDesc& d, const WarpSmem<TH>& sm, int lane, int y0, int rows,
+                                                int npx, size_t col_off, unsigned long long mask) {
+    using P = Px<DT>;
+    if (npx <= 0) return;
+    for (int r = 0; r < rows; ++r) {
+        if ((mask >> r) & 1ull) {
+            unsigned char* mrow = d.marker + (size_t)(y0 + r) * d.pitch_m + col_off;
+            const uint32_t w = sm.tm[(r + 1) * 32 + lane];
+            if (npx >= P::PPW) {
+                __stcg(reinterpret_cast<unsigned int*>(mrow), w);
+            } else {
+                uint32_t p[P::PPW];
+                P::unpack(w, p);
+#pragma unroll
+                for (int i = 0; i < P::PPW; ++i)
+                    if (i < npx) P::st_px(mrow + i * P::BPP, p[i]);
+            }
+        }
+    }
+}
+
+// Neighbour detection (MR.cu:366-512, pull form): the NB_* bits of the
+// neighbour tiles holding a pixel q next to a pixel p of this tile with
+// marker[q] < min(marker[p], mask[q]), looking only at the sides that rose.
+// The halo values in shared memory are the neighbours' pixels as fetched;
+// they can only have risen since, so a stale halo gives at most an extra
+// notification, never a missed one.
+template <int DT, int CONN, int TH>
+__device__ __forceinline__ unsigned detect_neighbours(const WarpSmem<TH>& sm, int lane, bool top_rose, bool bot_rose,
+                                                      bool side_rose) {
+    using P = Px<DT>;
+    unsigned nb = 0u;
+    uint32_t r0[P::PPW], r1[P::PPW], t_m[P::PPW], t_k[P::PPW], b_m[P::PPW], b_k[P::PPW];
+    P::unpack(sm.tm[32 + lane], r0);
+    P::unpack(sm.tm[TH * 32 + lane], r1);
+    P::unpack(sm.tm[lane], t_m);
+    P::unpack(sm.tk[lane], t_k);
+    P::unpack(sm.tm[(TH + 1) * 32 + lane], b_m);
+    P::unpack(sm.tk[(TH + 1) * 32 + lane], b_k);
+    uint32_t l0 = __shfl_up_sync(FULL, r0[P::PPW - 1], 1), n0 = __shfl_down_sync(FULL, r0[0], 1);
+    uint32_t l1 = __shfl_up_sync(FULL, r1[P::PPW - 1], 1), n1 = __shfl_down_sync(FULL, r1[0], 1);
+    if (lane == 0) l0 = l1 = P::MINPX;  // pixels of other tiles are not sources here
+    if (lane == 31) n0 = n1 = P::MINPX;
+    bool need_n = false, need_s = false;
+#pragma unroll
+    for (int j = 0; j < P::PPW; ++j) {
+        uint32_t v0 = r0[j], v1 = r1[j];
+        if (CONN == 8) {
+            v0 = P::mx3(j == 0 ? l0 : r0[j - 1], v0, j == P::PPW - 1 ? n0 : r0[j + 1]);
+            v1 = P::mx3(j == 0 ? l1 : r1[j - 1], v1, j == P::PPW - 1 ? n1 : r1[j + 1]);
+        }
+        need_n |= P::gt(P::mn(v0, t_k[j]), t_m[j]);
+        need_s |= P::gt(P::mn(v1, b_k[j]), b_m[j]);
+    }
+    if (top_rose && __any_sync(FULL, need_n)) nb |= NB_N;
+    if (bot_rose && __any_sync(FULL, need_s)) nb |= NB_S;
+
+    if (side_rose) {
+        // W / E: lanes walk the tile's first / last pixel column
+        bool need_w = false, need_e = false;
+        for (int r = 1 + lane; r <= TH; r += 32) {
+            uint32_t f[P::PPW], l[P::PPW];
+            P::unpack(sm.tm[r * 32], f);
+            P::unpack(sm.tm[r * 32 + 31], l);
+            uint32_t fv = f[0], lv = l[P::PPW - 1];
+            if (CONN == 8) {
+                uint32_t fa[P::PPW], la[P::PPW];
+                if (r > 1) {
+                    P::unpack(sm.tm[(r - 1) * 32], fa);
+                    P::unpack(sm.tm[(r - 1) * 32 + 31], la);
+                    fv = P::mx(fv, fa[0]);
+                    lv = P::mx(lv, la[P::PPW - 1]);
+                }
+                if (r < TH) {
+                    P::unpack(sm.tm[(r + 1) * 32], fa);
+                    P::unpack(sm.tm[(r + 1) * 32 + 31], la);
+                    fv = P::mx(fv, fa[0]);
+                    lv = P::mx(lv, la[P::PPW - 1]);
+                }
+            }
+            need_w |= P::gt(P::mn(fv, sm.hLk[r]), sm.hLm[r]);
+            need_e |= P::gt(P::mn(lv, sm.hRk[r]), sm.hRm[r]);
+        }
+        if (__any_sync(FULL, need_w)) nb |= NB_W;
+        if (__any_sync(FULL, need_e)) nb |= NB_E;
+    }
+    if (CONN == 8) {
+        uint32_t a[P::PPW], b[P::PPW], c[P::PPW], e[P::PPW];
+        P::unpack(sm.tm[32], a);
+        P::unpack(sm.tm[32 + 31], b);
+        P::unpack(sm.tm[TH * 32], c);
+        P::unpack(sm.tm[TH * 32 + 31], e);
+        if (top_rose && P::gt(P::mn(a[0], sm.hLk[0]), sm.hLm[0])) nb |= NB_NW;
+        if (top_rose && P::gt(P::mn(b[P::PPW - 1], sm.hRk[0]), sm.hRm[0])) nb |= NB_NE;
+        if (bot_rose && P::gt(P::mn(c[0], sm.hLk[TH + 1]), sm.hLm[TH + 1])) nb |= NB_SW;
+        if (bot_rose && P::gt(P::mn(e[P::PPW - 1], sm.hRk[TH + 1]), sm.hRm[TH + 1])) nb |= NB_SE;
+    }
+    return nb;
+}
+
+// Early flush that does nothing: the tile's neighbours are notified once,
+// after the visit.
+struct NoEarlyFlush {
+    static constexpr bool kEnabled = false;
+    bool use_passes;
+    __device__ bool passes(int) { return use_passes; }
+    __device__ bool want(int) { return false; }
+    __device__ void flush(unsigned, int) {}
+};
+
 // One warp: fetch tile (tx, ty) of image d with its one-pixel halo, run
 // raster / anti-raster sweeps until a sweep after the first changes nothing,
 // store the rows that rose, and report the neighbour tiles to notify: those
@@ -356,9 +660,16 @@ __device__ __forceinline__ uint32_t load_word_plain(const unsigned char* row, in
 // marker[q] < min(marker[p], mask[q]) where p's side of the tile rose.
 // `sides` (NB_* bits) names the halo sides whose pixels are new since the
 // tile last converged (all sides on a first visit).
-template <int DT, int CONN, int TH>
+//
+// `early` can publish intermediate results: after a sweep that raised a
+// boundary row or column, if early.want() says so (the engine asks for it
+// when the work queue runs dry, i.e. when the job is bound by its
+// propagation front), the rows risen so far are stored and the neighbours
+// they raise are handed to early.flush() while the sweeps go on.  The
+// returned `nb` then covers only what rose after the last flush.
+template <int DT, int CONN, int TH, class Early>
 __device__ __noinline__ VisitResult visit_tile(const ImgDesc& d, int tx, int ty, WarpSmem<TH>& sm, int lane,
-                                               unsigned& phase, long long timeout_ns, unsigned sides) {
+                                               unsigned& phase, long long timeout_ns, unsigned sides, Early& early) {
     using P = Px<DT>;
     constexpr int TW = 32 * P::PPW;
     VisitResult res{0u, 0u, 0u, true, 0, 0, 0};
@@ -444,140 +755,131 @@ __device__ __noinline__ VisitResult visit_tile(const ImgDesc& d, int tx, int ty,
     const long long c1 = clock64();
     res.t_fetch = c1 - c0;
 
-    // ---- local convergence (MR.cu:320-325, here with full-length scans):
-    // raster / anti-raster sweeps until a sweep after the first two changes
-    // nothing.  The first two sweeps also process the rows whose halo
-    // inputs are new: the top row for the raster sweep (N, NW, NE), the
-    // bottom row for the anti-raster sweep (S, SW, SE), every row when a
-    // side column that feeds the sweep changed (W, and E through the
-    // up-right / down-right diagonals for 8-connectivity; the reverse for
-    // the anti-raster sweep).
+    // ---- local convergence (MR.cu:320-325), by one of two solvers:
+    //   row sweeps (early.passes() false): raster / anti-raster sweeps, each
+    //     row a vertical update and a warp scan, until a sweep after the
+    //     first two changes nothing; fewest instructions per converged tile,
+    //     for when the GPU is full of work;
+    //   passes (early.passes() true): vertical and horizontal passes (see
+    //     vpass / hpass) until no rows are left whose constraints may be
+    //     violated; the shortest latency from a raised halo to a raised far
+    //     edge, for when the job is bound by its propagation front.
+    // Both are sequences of valid monotone updates that stop at the tile's
+    // fixed point, so they give the same bytes.
     constexpr unsigned long long ALL = TH == 64 ? ~0ull : ((1ull << TH) - 1ull);
     constexpr unsigned long long TOP = 1ull, BOT = 1ull << (TH - 1);
-    const unsigned side_down = CONN == 8 ? (NB_W | NB_E) : NB_W;
-    const unsigned side_up = CONN == 8 ? (NB_W | NB_E) : NB_E;
-    const unsigned long long force_down = (sides & side_down) ? ALL : (sides & (NB_N | NB_NW | NB_NE)) ? TOP : 0ull;
-    const unsigned long long force_up = (sides & side_up) ? ALL : (sides & (NB_S | NB_SW | NB_SE)) ? BOT : 0ull;
     const uint32_t edge_mask = lane == 0 ? P::FIRST_MASK : lane == 31 ? P::LAST_MASK : 0u;
-    unsigned long long rows_changed = 0ull, chg_prev = 0ull;
-    bool col_changed = false;
+    unsigned long long pend_rows = 0ull;  // rows risen since the last flush
+    bool col_changed = false;             // a side column rose since the last flush (per lane)
     unsigned sweeps = 0;
-    for (;;) {
-        unsigned long long dil = chg_prev | (chg_prev << 1) | (chg_prev >> 1);
-        if (sweeps == 0) dil |= force_down;
-        if (sweeps == 1) dil |= force_up;
-        dil &= ALL;
-        unsigned long long chg = 0ull;
-        if (dil != 0ull) {
-            if ((sweeps & 1u) == 0u)
-                sweep<DT, CONN, TH, true>(sm, lane, dil, chg, col_changed, edge_mask, res.row_steps);
-            else
-                sweep<DT, CONN, TH, false>(sm, lane, dil, chg, col_changed, edge_mask, res.row_steps);
+    long long t_flush = 0;
+    // After a pass that raised a boundary, with more passes to come: publish
+    // early if the engine asks for it.
+    auto maybe_flush = [&](unsigned long long chg, bool col_now) {
+        if (!Early::kEnabled) return;
+        const bool boundary = (chg & (TOP | BOT)) != 0ull || __any_sync(FULL, col_now);
+        if (!boundary || !early.want(lane)) return;
+        const long long f0 = clock64();
+        write_back_rows<DT, TH>(d, sm, lane, y0, rows, npx, col_off, pend_rows);
+        const unsigned nb = detect_neighbours<DT, CONN, TH>(sm, lane, (pend_rows & TOP) != 0ull,
+                                                            (pend_rows & BOT) != 0ull, __any_sync(FULL, col_changed));
+        __syncwarp();
+        if (nb != 0u) early.flush(nb, lane);
+        pend_rows = 0ull;
+        col_changed = false;
+        t_flush += clock64() - f0;
+    };
+    if (!early.passes(lane)) {
+        // Rows whose halo inputs are new are processed by the first two
+        // sweeps: the top row by the raster sweep (N, NW, NE), the bottom row
+        // by the anti-raster sweep (S, SW, SE), every row when a side column
+        // that feeds the sweep changed (W, and E through the up-right /
+        // down-right diagonals for 8-connectivity; the reverse for the
+        // anti-raster sweep).  Other rows are skipped while nothing they
+        // depend on has changed.
+        const unsigned side_down = CONN == 8 ? (NB_W | NB_E) : NB_W;
+        const unsigned side_up = CONN == 8 ? (NB_W | NB_E) : NB_E;
+        const unsigned long long force_down =
+            (sides & side_down) ? ALL : (sides & (NB_N | NB_NW | NB_NE)) ? TOP : 0ull;
+        const unsigned long long force_up = (sides & side_up) ? ALL : (sides & (NB_S | NB_SW | NB_SE)) ? BOT : 0ull;
+        unsigned long long chg_prev = 0ull;
+        for (;;) {
+            unsigned long long dil = chg_prev | (chg_prev << 1) | (chg_prev >> 1);
+            if (sweeps == 0) dil |= force_down;
+            if (sweeps == 1) dil |= force_up;
+            dil &= ALL;
+            unsigned long long chg = 0ull;
+            bool col_now = false;
+            if (dil != 0ull) {
+                if ((sweeps & 1u) == 0u)
+                    sweep<DT, CONN, TH, true>(sm, lane, dil, chg, col_now, edge_mask, res.row_steps);
+                else
+                    sweep<DT, CONN, TH, false>(sm, lane, dil, chg, col_now, edge_mask, res.row_steps);
+            }
+            ++sweeps;
+            pend_rows |= chg;
+            col_changed |= col_now;
+            chg_prev = chg;
+            if (chg == 0ull && sweeps >= 2) break;
+            if (chg != 0ull) maybe_flush(chg, col_now);
         }
-        ++sweeps;
-        rows_changed |= chg;
-        chg_prev = chg;
-        if (chg == 0ull && sweeps >= 2) break;
+    } else {
+        // dVd / dVu: rows whose constraint towards the row above / below may
+        // be violated; dH: rows whose horizontal constraints may be violated.
+        // A first visit has every row dirty; a revisit only the rows fed by
+        // the halo sides that rose: N (and the N corners) the top row for the
+        // downward pass, S the bottom row for the upward pass, W / E every
+        // row for the horizontal pass and, with 8-connectivity, for both
+        // vertical passes (their diagonals read the side columns).
+        const bool fresh = sides == 0xffu;
+        const bool side_we = (sides & (NB_W | NB_E)) != 0u;
+        unsigned long long dVd = (sides & (NB_N | NB_NW | NB_NE)) ? TOP : 0ull;
+        unsigned long long dVu = (sides & (NB_S | NB_SW | NB_SE)) ? BOT : 0ull;
+        unsigned long long dH = side_we ? ALL : 0ull;
+        if (fresh || (CONN == 8 && side_we)) dVd = dVu = ALL;
+        for (int it = 0; (dVd | dVu | dH) != 0ull; it = (it + 1) & 3) {
+            unsigned long long chg;
+            bool col_now = false;
+            if (it == 0) {
+                if (dVd == 0ull) continue;
+                chg = vpass<DT, CONN, TH, true>(sm, lane, dVd, edge_mask, col_now, res.row_steps);
+                dVd = 0ull;
+                dVu |= chg >> 1;
+                dH |= chg;
+            } else if (it == 2) {
+                if (dVu == 0ull) continue;
+                chg = vpass<DT, CONN, TH, false>(sm, lane, dVu, edge_mask, col_now, res.row_steps);
+                dVu = 0ull;
+                dVd |= (chg << 1) & ALL;
+                dH |= chg;
+            } else {
+                if (dH == 0ull) continue;
+                unsigned blocks = 0u;
+                chg = hpass<DT, TH>(sm, lane, dH, edge_mask, col_now, blocks);
+                res.row_steps += 4u * blocks;
+                dH = 0ull;
+                dVd |= (chg << 1) & ALL;
+                dVu |= chg >> 1;
+            }
+            ++sweeps;
+            pend_rows |= chg;
+            col_changed |= col_now;
+            if (chg != 0ull && (dVd | dVu | dH) != 0ull) maybe_flush(chg, col_now);
+        }
     }
     res.sweeps = sweeps;
     const long long c2 = clock64();
-    res.t_proc = c2 - c1;
-    if (rows_changed == 0ull) return res;  // nothing rose: nothing to store or notify
+    res.t_proc = c2 - c1 - t_flush;
+    res.t_dump = t_flush;
+    if (pend_rows == 0ull) return res;  // nothing rose since the last flush: nothing to store or notify
 
-    // ---- write back the rows that rose (own tile only; MR.cu:335-364)
-    if (npx > 0) {
-        for (int r = 0; r < rows; ++r) {
-            if ((rows_changed >> r) & 1ull) {
-                unsigned char* mrow = d.marker + (size_t)(y0 + r) * d.pitch_m + col_off;
-                const uint32_t w = sm.tm[(r + 1) * 32 + lane];
-                if (npx >= P::PPW) {
-                    __stcg(reinterpret_cast<unsigned int*>(mrow), w);
-                } else {
-                    uint32_t p[P::PPW];
-                    P::unpack(w, p);
-#pragma unroll
-                    for (int i = 0; i < P::PPW; ++i)
-                        if (i < npx) P::st_px(mrow + i * P::BPP, p[i]);
-                }
-            }
-        }
-    }
-
-    // ---- neighbour detection (MR.cu:366-512, pull form)
-    const bool top_rose = rows_changed & 1ull;
-    const bool bot_rose = (rows_changed >> (TH - 1)) & 1ull;
-    const bool side_rose = __any_sync(FULL, col_changed);
-    unsigned nb = 0u;
-    {
-        uint32_t r0[P::PPW], r1[P::PPW], t_m[P::PPW], t_k[P::PPW], b_m[P::PPW], b_k[P::PPW];
-        P::unpack(sm.tm[32 + lane], r0);
-        P::unpack(sm.tm[TH * 32 + lane], r1);
-        P::unpack(sm.tm[lane], t_m);
-        P::unpack(sm.tk[lane], t_k);
-        P::unpack(sm.tm[(TH + 1) * 32 + lane], b_m);
-        P::unpack(sm.tk[(TH + 1) * 32 + lane], b_k);
-        uint32_t l0 = __shfl_up_sync(FULL, r0[P::PPW - 1], 1), n0 = __shfl_down_sync(FULL, r0[0], 1);
-        uint32_t l1 = __shfl_up_sync(FULL, r1[P::PPW - 1], 1), n1 = __shfl_down_sync(FULL, r1[0], 1);
-        if (lane == 0) l0 = l1 = P::MINPX;  // pixels of other tiles are not sources here
-        if (lane == 31) n0 = n1 = P::MINPX;
-        bool need_n = false, need_s = false;
-#pragma unroll
-        for (int j = 0; j < P::PPW; ++j) {
-            uint32_t v0 = r0[j], v1 = r1[j];
-            if (CONN == 8) {
-                v0 = P::mx3(j == 0 ? l0 : r0[j - 1], v0, j == P::PPW - 1 ? n0 : r0[j + 1]);
-                v1 = P::mx3(j == 0 ? l1 : r1[j - 1], v1, j == P::PPW - 1 ? n1 : r1[j + 1]);
-            }
-            need_n |= P::gt(P::mn(v0, t_k[j]), t_m[j]);
-            need_s |= P::gt(P::mn(v1, b_k[j]), b_m[j]);
-        }
-        if (top_rose && __any_sync(FULL, need_n)) nb |= NB_N;
-        if (bot_rose && __any_sync(FULL, need_s)) nb |= NB_S;
-
-        if (side_rose) {
-            // W / E: lanes walk the tile's first / last pixel column
-            bool need_w = false, need_e = false;
-            for (int r = 1 + lane; r <= TH; r += 32) {
-                uint32_t f[P::PPW], l[P::PPW];
-                P::unpack(sm.tm[r * 32], f);
-                P::unpack(sm.tm[r * 32 + 31], l);
-                uint32_t fv = f[0], lv = l[P::PPW - 1];
-                if (CONN == 8) {
-                    uint32_t fa[P::PPW], la[P::PPW];
-                    if (r > 1) {
-                        P::unpack(sm.tm[(r - 1) * 32], fa);
-                        P::unpack(sm.tm[(r - 1) * 32 + 31], la);
-                        fv = P::mx(fv, fa[0]);
-                        lv = P::mx(lv, la[P::PPW - 1]);
-                    }
-                    if (r < TH) {
-                        P::unpack(sm.tm[(r + 1) * 32], fa);
-                        P::unpack(sm.tm[(r + 1) * 32 + 31], la);
-                        fv = P::mx(fv, fa[0]);
-                        lv = P::mx(lv, la[P::PPW - 1]);
-                    }
-                }
-                need_w |= P::gt(P::mn(fv, sm.hLk[r]), sm.hLm[r]);
-                need_e |= P::gt(P::mn(lv, sm.hRk[r]), sm.hRm[r]);
-            }
-            if (__any_sync(FULL, need_w)) nb |= NB_W;
-            if (__any_sync(FULL, need_e)) nb |= NB_E;
-        }
-        if (CONN == 8) {
-            uint32_t a[P::PPW], b[P::PPW], c[P::PPW], e[P::PPW];
-            P::unpack(sm.tm[32], a);
-            P::unpack(sm.tm[32 + 31], b);
-            P::unpack(sm.tm[TH * 32], c);
-            P::unpack(sm.tm[TH * 32 + 31], e);
-            if (top_rose && P::gt(P::mn(a[0], sm.hLk[0]), sm.hLm[0])) nb |= NB_NW;
-            if (top_rose && P::gt(P::mn(b[P::PPW - 1], sm.hRk[0]), sm.hRm[0])) nb |= NB_NE;
-            if (bot_rose && P::gt(P::mn(c[0], sm.hLk[TH + 1]), sm.hLm[TH + 1])) nb |= NB_SW;
-            if (bot_rose && P::gt(P::mn(e[P::PPW - 1], sm.hRk[TH + 1]), sm.hRm[TH + 1])) nb |= NB_SE;
-        }
-    }
+    // ---- write back the rows that rose, then neighbour detection
+    write_back_rows<DT, TH>(d, sm, lane, y0, rows, npx, col_off, pend_rows);
+    const unsigned nb = detect_neighbours<DT, CONN, TH>(sm, lane, (pend_rows & TOP) != 0ull,
+                                                        (pend_rows & BOT) != 0ull, __any_sync(FULL, col_changed));
     __syncwarp();
     res.nb = nb;
-    res.t_dump = clock64() - c2;
+    res.t_dump += clock64() - c2;
     return res;
 }
 

@@ -24,17 +24,18 @@ __device__ __forceinline__ int find_image(const EngineArgs& a, unsigned g) {
     return lo;
 }
 
-template <int TH>
+template <int TH, class Early>
 __device__ __forceinline__ VisitResult dispatch_visit(const ImgDesc& d, int tx, int ty, WarpSmem<TH>& sm, int lane,
-                                                     unsigned& phase, long long timeout_ns, unsigned sides) {
+                                                     unsigned& phase, long long timeout_ns, unsigned sides,
+                                                     Early& early) {
     const int mode = d.dtype * 2 + (d.conn == 8 ? 1 : 0);
     switch (mode) {
-        case 0: return visit_tile<DT_U8, 4, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides);
-        case 1: return visit_tile<DT_U8, 8, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides);
-        case 2: return visit_tile<DT_U16, 4, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides);
-        case 3: return visit_tile<DT_U16, 8, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides);
-        case 4: return visit_tile<DT_I32, 4, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides);
-        default: return visit_tile<DT_I32, 8, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides);
+        case 0: return visit_tile<DT_U8, 4, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides, early);
+        case 1: return visit_tile<DT_U8, 8, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides, early);
+        case 2: return visit_tile<DT_U16, 4, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides, early);
+        case 3: return visit_tile<DT_U16, 8, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides, early);
+        case 4: return visit_tile<DT_I32, 4, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides, early);
+        default: return visit_tile<DT_I32, 8, TH>(d, tx, ty, sm, lane, phase, timeout_ns, sides, early);
     }
 }
 
@@ -151,7 +152,7 @@ __device__ void push_entries(const EngineArgs& a, bool want, unsigned gn, int la
 // trip through the queue.  Returns ~0u when there is none.
 template <int VAR>
 __device__ unsigned notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty, unsigned nb, int lane, unsigned* wq,
-                           WarpCounters& cnt) {
+                           WarpCounters& cnt, bool keep_one = true) {
     bool want = false;
     unsigned gn = 0u;
     if (lane < 8 && ((nb >> lane) & 1u)) {
@@ -164,7 +165,7 @@ __device__ unsigned notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty
         }
     }
     unsigned cont = ~0u;
-    if (VAR == VAR_ASYNC) {
+    if (VAR == VAR_ASYNC && keep_one) {
         const unsigned ballot = __ballot_sync(FULL, want);
         if (ballot != 0u) {
             const int leader = __ffs(ballot) - 1;
@@ -175,6 +176,40 @@ __device__ unsigned notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty
     push_entries<VAR>(a, want, gn, lane, wq, cnt);
     return cont;
 }
+
+// Early publication for the async queue: while many warps wait for work
+// (the job is bound by its propagation front), a visit that raised a
+// boundary of its tile stores what it has and notifies those neighbours at
+// once instead of after its last sweep, so they can start while this tile is
+// still converging.  While the warps are busy it would only add revisits.
+template <int VAR>
+struct EarlyFlush {
+    static constexpr bool kEnabled = VAR == VAR_ASYNC;
+    const EngineArgs* a;
+    const ImgDesc* d;
+    int tx, ty;
+    WarpCounters* cnt;
+    bool use_passes;  // in-tile solver of this visit
+    // Front-bound: more than half of the grid's warps have claimed a ring
+    // position that no producer has filled yet (they wait for work).  A
+    // quarter or an eighth switches too early on h-dome images, three
+    // quarters too late on long corridors.
+    __device__ static bool sample(const EngineArgs& a, int lane) {
+        unsigned v = 0u;
+        if (lane == 0) {
+            const unsigned head = ld_volatile(&a.ctrl->ahead), tail = ld_volatile(&a.ctrl->atail);
+            v = (int)(head - tail) > (int)(gridDim.x * (unsigned)kWarps / 2u) ? 1u : 0u;
+        }
+        return __shfl_sync(FULL, v, 0) != 0u;
+    }
+    __device__ bool passes(int) { return use_passes; }
+    __device__ bool want(int lane) { return sample(*a, lane); }
+    __device__ void flush(unsigned nb, int lane) {
+        __threadfence();  // release: the rows just stored before the neighbours' DIRTY
+        __syncwarp();
+        notify<VAR>(*a, *d, tx, ty, nb, lane, nullptr, *cnt, false);
+    }
+};
 
 // ------------------------------------------------------------ one entry
 // Takes tile g unless another warp owns it (that owner sees DIRTY when it
@@ -201,7 +236,19 @@ __device__ bool process_entry(const EngineArgs& a, unsigned g, WarpSmem<TH>& sm,
         const ImgDesc d = a.imgs[ii];
         const int t = (int)(g - (unsigned)d.tile_base);
         const int ty = t / d.tiles_x, tx = t - ty * d.tiles_x;
-        const VisitResult r = dispatch_visit<TH>(d, tx, ty, sm, lane, phase, a.timeout_ns, sides);
+        // In-tile solver: row sweeps (fewest instructions) while the warps
+        // are busy, passes (shortest latency) while many wait for work (async
+        // queue; the round-based queues use the sweeps unless told otherwise).
+        bool use_passes = a.solver == 2;
+        if (a.solver == 0 && VAR == VAR_ASYNC) use_passes = EarlyFlush<VAR_ASYNC>::sample(a, lane);
+        VisitResult r;
+        if (VAR == VAR_ASYNC) {
+            EarlyFlush<VAR> early{&a, &d, tx, ty, &cnt, use_passes};
+            r = dispatch_visit<TH>(d, tx, ty, sm, lane, phase, a.timeout_ns, sides, early);
+        } else {
+            NoEarlyFlush early{use_passes};
+            r = dispatch_visit<TH>(d, tx, ty, sm, lane, phase, a.timeout_ns, sides, early);
+        }
         if (!r.ok) {
             if (lane == 0) set_error(a.ctrl, DEV_ERR_TIMEOUT);
             return false;

@@ -77,6 +77,7 @@ struct EngineArgs {
     Ctrl* ctrl;
     long long timeout_ns;
     int max_restarts;
+    int solver;  // 0 automatic, 1 row sweeps, 2 passes
 };
 
 }  // namespace iwpp

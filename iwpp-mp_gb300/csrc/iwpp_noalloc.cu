@@ -123,6 +123,7 @@ extern "C" int iwpp_reconstruct_noalloc(void* marker, const void* mask, size_t p
     a.ctrl = reinterpret_cast<Ctrl*>(base);
     a.timeout_ns = 10000ll * 1000000ll;
     a.max_restarts = 64;
+    a.solver = 0;
 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     LaunchInfo li;

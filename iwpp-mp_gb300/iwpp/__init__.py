@@ -41,13 +41,14 @@ class IwppError(RuntimeError):
 class Config(ctypes.Structure):
     _fields_ = [("tile_rows", ctypes.c_int), ("queue_capacity", ctypes.c_longlong),
                 ("init_passes", ctypes.c_int), ("grid_ctas", ctypes.c_int), ("max_restarts", ctypes.c_int),
-                ("timeout_ms", ctypes.c_int), ("clip_marker", ctypes.c_int), ("plain_loads", ctypes.c_int)]
+                ("timeout_ms", ctypes.c_int), ("clip_marker", ctypes.c_int), ("plain_loads", ctypes.c_int),
+                ("solver", ctypes.c_int)]
 
     @classmethod
     def make(cls, tile_rows=0, queue_capacity=0, init_passes=-1, grid_ctas=0, max_restarts=0, timeout_ms=0,
-             clip_marker=0, plain_loads=0):
+             clip_marker=0, plain_loads=0, solver=0):
         return cls(tile_rows, queue_capacity, init_passes, grid_ctas, max_restarts, timeout_ms, clip_marker,
-                   plain_loads)
+                   plain_loads, solver)
 
 
 class Stats(ctypes.Structure):
