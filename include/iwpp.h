@@ -52,9 +52,13 @@ typedef enum iwpp_queue_variant {
                                 (lock-free ring, fetch-and-add claims) */
 } iwpp_queue_variant;
 
+/* Fields left at their defaults (tile_rows 0, queue_capacity 0,
+ * init_passes -1, solver 0; or cfg NULL) are taken from the tuning table
+ * when it holds an entry for the job's workload class (iwpp_autotune). */
 typedef struct iwpp_config {
-    int tile_rows;             /* 32 or 64 rows per tile; 0 = default (autotuner table) */
-    long long queue_capacity;  /* entries per queue buffer; 0 = default */
+    int tile_rows;             /* 32 or 64 rows per tile; 0 = default (64) */
+    long long queue_capacity;  /* entries per queue buffer; 0 = default; < 0: that multiple
+                                  of the job's tile count */
     int init_passes;           /* whole-image raster + anti-raster pairs first; -1 = default */
     int grid_ctas;             /* persistent grid size; 0 = one full wave */
     int max_restarts;          /* queue-overflow restarts allowed; 0 = default (64) */
@@ -139,6 +143,38 @@ IWPP_API int iwpp_plan_create(iwpp_plan *out, iwpp_handle h, const iwpp_image *i
 IWPP_API int iwpp_plan_launch(iwpp_plan p, void *stream);
 IWPP_API int iwpp_plan_sync(iwpp_plan p, iwpp_stats *stats);
 IWPP_API int iwpp_plan_destroy(iwpp_plan p);
+
+/* ---- autotuner ------------------------------------------------------------ */
+/* No counterpart in the reference (its tile size, queue sizes and number of
+ * initial passes are compile-time constants, IWPP MP/include/
+ * MorphologicalReconstruction.cuh:6-7, and commented-out sweeps, MR.cu:792-795).
+ * Times candidate configurations on the caller's own batch -- tile rows
+ * 64 / 32 x in-tile solver, then 1 / 2 initial raster + anti-raster pass
+ * pairs, then (mutex / double queues) queue capacity 1x / 16x the tiles --
+ * each the median of `repeats` runs (0 = 3) from the same markers, records
+ * the fastest in the process-wide tuning table under the batch's workload
+ * class (queue variant, pixel type, connectivity, floor(log2(pixels)),
+ * single image or batch) and returns it.  On success the markers hold the
+ * reconstruction; on failure they are as they came. */
+typedef struct iwpp_tune_result {
+    iwpp_config best;  /* fastest configuration */
+    double best_ms;    /* its median device time */
+    double default_ms; /* median device time of the untuned default (64 rows, automatic solver) */
+    int candidates;    /* configurations timed */
+    int reserved;
+} iwpp_tune_result;
+IWPP_API int iwpp_autotune(iwpp_handle h, const iwpp_image *images, int n, int variant, int repeats, void *stream,
+                           iwpp_tune_result *out);
+/* The tuning table as text (one line per class); load merges, a malformed
+ * file changes nothing. */
+IWPP_API int iwpp_tune_save(const char *path);
+IWPP_API int iwpp_tune_load(const char *path);
+IWPP_API int iwpp_tune_clear(void);
+IWPP_API int iwpp_tune_entries(void);
+/* The entry for one image class (batch 0) or batch class (batch 1), as a
+ * config; IWPP_ERR_INVALID when there is none. */
+IWPP_API int iwpp_tune_lookup(int variant, int dtype, int connectivity, long long pixels, int batch,
+                              iwpp_config *out);
 
 /* ---- precondition helper (replaces the reference's clipImage kernel,
  *      IWPP MP/src/MorphologicalReconstruction.cu:827-836) ----------------- */

@@ -16,6 +16,7 @@
 
 #include "iwpp.h"
 #include "iwpp_engine.cuh"
+#include "iwpp_tune.h"
 
 using namespace iwpp;
 
@@ -53,7 +54,7 @@ int resolve_variant(int variant) {
 
 struct Config {
     int tile_rows;
-    long long queue_capacity;
+    long long queue_capacity;  // < 0: that multiple of the job's tile count
     int init_passes;
     int grid_ctas;
     int max_restarts;
@@ -61,12 +62,14 @@ struct Config {
     int clip_marker;
     int plain_loads;
     int solver;
+    // fields the caller left at their defaults (the tuning table may fill them)
+    bool dflt_tile, dflt_queue, dflt_init, dflt_solver;
 };
 
 Config resolve_config(const iwpp_config* c) {
     Config r;
     r.tile_rows = c && (c->tile_rows == 32 || c->tile_rows == 64) ? c->tile_rows : 0;
-    r.queue_capacity = c && c->queue_capacity > 0 ? c->queue_capacity : 0;
+    r.queue_capacity = c && c->queue_capacity != 0 ? c->queue_capacity : 0;
     r.init_passes = c && c->init_passes >= 0 ? c->init_passes : 0;
     r.grid_ctas = c && c->grid_ctas > 0 ? c->grid_ctas : 0;
     r.max_restarts = c && c->max_restarts > 0 ? c->max_restarts : 64;
@@ -74,6 +77,10 @@ Config resolve_config(const iwpp_config* c) {
     r.clip_marker = c ? c->clip_marker : 0;
     r.plain_loads = c ? c->plain_loads : 0;
     r.solver = c && c->solver >= 0 && c->solver <= 2 ? c->solver : 0;
+    r.dflt_tile = r.tile_rows == 0;
+    r.dflt_queue = r.queue_capacity == 0;
+    r.dflt_init = !c || c->init_passes < 0;
+    r.dflt_solver = r.solver == 0;
     if (std::getenv("IWPP_PLAIN_LOADS")) r.plain_loads = 1;
     return r;
 }
@@ -204,6 +211,14 @@ struct Job {
     Config cfg;
 };
 
+// Queue entries of a job: the variant's rule applied to the requested
+// capacity (negative: that multiple of the job's tiles).
+long long job_queue_capacity(const Job& job) {
+    const long long req = job.cfg.queue_capacity < 0 ? -job.cfg.queue_capacity * std::max(job.G, 1ll)
+                                                     : job.cfg.queue_capacity;
+    return queue_capacity_for(job.variant, job.G, req);
+}
+
 // How images whose rows are not 4-byte aligned are handled.
 enum StageMode { STAGE_REJECT = 0, STAGE_ASYNC = 1, STAGE_OWNED = 2 };
 
@@ -211,9 +226,29 @@ enum StageMode { STAGE_REJECT = 0, STAGE_ASYNC = 1, STAGE_OWNED = 2 };
 // finish_staging.  STAGE_OWNED: plain allocations owned by the caller (a
 // plan), copies left to the caller.
 int build_job(Job& job, const iwpp_image* imgs, int n, int variant, const iwpp_config* cfgp, cudaStream_t s,
-              int staging) {
+              int staging, bool use_table = true) {
     job.cfg = resolve_config(cfgp);
     job.variant = resolve_variant(variant);
+    if (use_table && n > 0 && (job.cfg.dflt_tile || job.cfg.dflt_queue || job.cfg.dflt_init || job.cfg.dflt_solver)) {
+        // fields left at their defaults come from the tuning table, if it
+        // has an entry for this workload class
+        std::vector<int> dts, cns;
+        std::vector<long long> pxs;
+        for (int i = 0; i < n; ++i) {
+            if (imgs[i].width <= 0 || imgs[i].height <= 0) continue;
+            dts.push_back(imgs[i].dtype);
+            cns.push_back(imgs[i].connectivity);
+            pxs.push_back((long long)imgs[i].width * imgs[i].height);
+        }
+        TuneEntry e;
+        if (!dts.empty() &&
+            tune_lookup(tune_key(job.variant, dts.data(), cns.data(), pxs.data(), (int)dts.size()), &e)) {
+            if (job.cfg.dflt_tile) job.cfg.tile_rows = e.tile_rows;
+            if (job.cfg.dflt_solver) job.cfg.solver = e.solver;
+            if (job.cfg.dflt_init) job.cfg.init_passes = e.init_passes;
+            if (job.cfg.dflt_queue && e.queue_mult > 0) job.cfg.queue_capacity = -(long long)e.queue_mult;
+        }
+    }
     int th = job.cfg.tile_rows;
     if (th == 0) th = n > 0 ? default_tile_rows(imgs[0].dtype) : 64;
     job.tile_rows = th;
@@ -396,7 +431,7 @@ int check_device(int device) {
 int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool use_events, cudaEvent_t ev0,
                 cudaEvent_t ev1, bool upload_descs) {
     const bool two = job.variant == IWPP_QUEUE_DOUBLE || job.variant == IWPP_QUEUE_UNIQUE;
-    const long long cap = queue_capacity_for(job.variant, job.G, job.cfg.queue_capacity);
+    const long long cap = job_queue_capacity(job);
     const Layout l = layout_for((long long)job.descs.size(), job.G, cap, two);
     int rc = ensure_workspace(ws, l.total);
     if (rc != IWPP_OK) return rc;
@@ -554,6 +589,8 @@ int run_job_sync(iwpp_handle h, const iwpp_image* imgs, int n, int variant, cons
 }  // namespace
 
 namespace iwpp {
+int resolve_queue_variant(int variant) { return resolve_variant(variant); }
+
 // Grows a handle's workspace ahead of use (the server sizes each lane once).
 int handle_reserve(iwpp_handle h, size_t bytes) {
     if (!h) return IWPP_ERR_INVALID;
@@ -627,7 +664,7 @@ int iwpp_handle_destroy(iwpp_handle h) {
 
 long long iwpp_workspace_bytes(long long tiles, int variant, long long queue_capacity) {
     const int v = resolve_variant(variant);
-    const long long cap = queue_capacity_for(v, tiles, queue_capacity);
+    const long long cap = queue_capacity_for(v, tiles, queue_capacity < 0 ? -queue_capacity * tiles : queue_capacity);
     return (long long)layout_for(1, tiles, cap, v == IWPP_QUEUE_DOUBLE || v == IWPP_QUEUE_UNIQUE).total;
 }
 
@@ -741,7 +778,7 @@ int iwpp_plan_create(iwpp_plan* out, iwpp_handle h, const iwpp_image* images, in
     if (rc == IWPP_OK) {
         // Workspace and descriptors first (outside the graph, once).
         const bool two = job.variant == IWPP_QUEUE_DOUBLE || job.variant == IWPP_QUEUE_UNIQUE;
-        const long long cap = queue_capacity_for(job.variant, job.G, job.cfg.queue_capacity);
+        const long long cap = job_queue_capacity(job);
         const Layout l = layout_for((long long)job.descs.size(), job.G, cap, two);
         rc = ensure_workspace(p->ws, l.total);
         if (rc == IWPP_OK && !job.descs.empty()) {
@@ -843,6 +880,159 @@ int iwpp_plan_destroy(iwpp_plan p) {
     }
     delete p;
     return IWPP_OK;
+}
+
+int iwpp_autotune(iwpp_handle h, const iwpp_image* images, int n, int variant, int repeats, void* stream,
+                  iwpp_tune_result* out) {
+    if (!h || n <= 0 || !images || repeats < 0 || repeats > 50) return set_last(IWPP_ERR_INVALID);
+    for (int i = 0; i < n; ++i) {
+        const iwpp_image& im = images[i];
+        const int rc = check_image(im.marker, im.mask, im.pitch_marker, im.pitch_mask, im.width, im.height, im.dtype,
+                                   im.connectivity);
+        if (rc != IWPP_OK) return set_last(rc);
+    }
+    if (repeats == 0) repeats = 3;
+    std::lock_guard<std::mutex> lk(h->mu);
+    int prev_dev = 0;
+    cudaGetDevice(&prev_dev);
+    if (prev_dev != h->device) cudaSetDevice(h->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int v = resolve_variant(variant);
+
+    // pristine copies of the markers: every candidate starts from them
+    std::vector<void*> saved((size_t)n, nullptr);
+    int rc = IWPP_OK;
+    for (int i = 0; i < n && rc == IWPP_OK; ++i) {
+        const iwpp_image& im = images[i];
+        if (im.width == 0 || im.height == 0) continue;
+        const size_t row = (size_t)im.width * bpp_of(im.dtype);
+        cudaError_t e = cudaMallocAsync(&saved[(size_t)i], row * im.height, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpy2DAsync(saved[(size_t)i], row, im.marker, im.pitch_marker, row, im.height,
+                                  cudaMemcpyDeviceToDevice, s);
+        rc = cuda_status(e);
+    }
+    auto restore = [&]() -> int {
+        for (int i = 0; i < n; ++i) {
+            const iwpp_image& im = images[i];
+            if (!saved[(size_t)i]) continue;
+            const size_t row = (size_t)im.width * bpp_of(im.dtype);
+            cudaError_t e = cudaMemcpy2DAsync(im.marker, im.pitch_marker, saved[(size_t)i], row, row, im.height,
+                                              cudaMemcpyDeviceToDevice, s);
+            if (e != cudaSuccess) return cuda_status(e);
+        }
+        return IWPP_OK;
+    };
+    // median device time of one configuration, or a negative value when it failed
+    int timed = 0;
+    auto measure = [&](const iwpp_config& c) -> double {
+        std::vector<float> ts;
+        for (int r = 0; r < repeats; ++r) {
+            if (restore() != IWPP_OK) return -1.0;
+            Job job;
+            int jrc = build_job(job, images, n, v, &c, s, STAGE_ASYNC, false);
+            if (jrc == IWPP_OK) jrc = enqueue_job(job, h->ws, s, h->device, true, h->ev0, h->ev1, true);
+            const int src = finish_staging(job, s);
+            if (jrc == IWPP_OK) jrc = src;
+            if (jrc != IWPP_OK) {
+                cudaStreamSynchronize(s);
+                return -1.0;
+            }
+            if (cudaStreamSynchronize(s) != cudaSuccess) return -1.0;
+            if (read_stats(h->host_ctrl, h->ws, s, job.G, job.variant, nullptr, 0.f) != IWPP_OK) return -1.0;
+            float ms = 0.f;
+            if (job.G > 0) cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+            ts.push_back(ms);
+        }
+        ++timed;
+        std::sort(ts.begin(), ts.end());
+        return ts[ts.size() / 2];
+    };
+
+    iwpp_config best{};
+    best.init_passes = 0;
+    best.tile_rows = 64;
+    double best_ms = -1.0, default_ms = -1.0;
+    auto consider = [&](const iwpp_config& c, bool is_default) {
+        const double ms = measure(c);
+        if (ms < 0.0) return;
+        if (is_default) default_ms = ms;
+        if (best_ms < 0.0 || ms < best_ms) {
+            best_ms = ms;
+            best = c;
+        }
+    };
+    if (rc == IWPP_OK) {
+        // stage 1: tile height x in-tile solver, no initial passes
+        for (int th : {64, 32})
+            for (int solver : {0, 1, 2}) {
+                iwpp_config c{};
+                c.tile_rows = th;
+                c.solver = solver;
+                c.init_passes = 0;
+                consider(c, th == 64 && solver == 0);
+            }
+        // stage 2: initial whole-image raster / anti-raster pass pairs
+        if (best_ms >= 0.0) {
+            const iwpp_config base = best;
+            for (int ip : {1, 2}) {
+                iwpp_config c = base;
+                c.init_passes = ip;
+                consider(c, false);
+            }
+        }
+        // stage 3: queue capacity, for the queues whose capacity is free
+        if (best_ms >= 0.0 && (v == IWPP_QUEUE_MUTEX || v == IWPP_QUEUE_DOUBLE)) {
+            const iwpp_config base = best;
+            for (int mult : {1, 16}) {
+                iwpp_config c = base;
+                c.queue_capacity = -mult;
+                consider(c, false);
+            }
+        }
+        if (best_ms < 0.0) rc = IWPP_ERR_TIMEOUT;
+    }
+    if (rc == IWPP_OK) {
+        // record the winner for this workload class
+        std::vector<int> dts, cns;
+        std::vector<long long> pxs;
+        for (int i = 0; i < n; ++i) {
+            if (images[i].width <= 0 || images[i].height <= 0) continue;
+            dts.push_back(images[i].dtype);
+            cns.push_back(images[i].connectivity);
+            pxs.push_back((long long)images[i].width * images[i].height);
+        }
+        if (!dts.empty()) {
+            TuneEntry e{best.tile_rows, best.solver, best.init_passes,
+                        best.queue_capacity < 0 ? (int)-best.queue_capacity : 0};
+            tune_store(tune_key(v, dts.data(), cns.data(), pxs.data(), (int)dts.size()), e);
+        }
+        // leave the images reconstructed (with the winner)
+        rc = restore();
+        if (rc == IWPP_OK) {
+            Job job;
+            rc = build_job(job, images, n, v, &best, s, STAGE_ASYNC, false);
+            if (rc == IWPP_OK) rc = enqueue_job(job, h->ws, s, h->device, false, h->ev0, h->ev1, true);
+            const int src = finish_staging(job, s);
+            if (rc == IWPP_OK) rc = src;
+            if (cudaStreamSynchronize(s) != cudaSuccess && rc == IWPP_OK) rc = IWPP_ERR_CUDA;
+            if (rc == IWPP_OK) rc = read_stats(h->host_ctrl, h->ws, s, job.G, job.variant, nullptr, 0.f);
+        }
+    } else {
+        restore();  // leave the markers as they came
+    }
+    for (void* p : saved)
+        if (p) cudaFreeAsync(p, s);
+    cudaStreamSynchronize(s);
+    if (out) {
+        out->best = best;
+        out->best_ms = best_ms;
+        out->default_ms = default_ms;
+        out->candidates = timed;
+        out->reserved = 0;
+    }
+    if (prev_dev != h->device) cudaSetDevice(prev_dev);
+    return set_last(rc);
 }
 
 int iwpp_clip(void* marker, const void* mask, size_t pitch_marker, size_t pitch_mask, int width, int height,

@@ -1,0 +1,34 @@
+// iwpp_tune.h -- the process-wide tuning table (internal to libiwpp).
+//
+// Entries map a workload class to the configuration the autotuner found
+// fastest for it.  The class is (queue variant, pixel type, connectivity,
+// pixel-count class = floor(log2(total pixels)), single image or batch);
+// a batch of mixed types or connectivities uses -1 for that field.
+#pragma once
+
+#include <string>
+
+namespace iwpp {
+
+struct TuneKey {
+    int variant;
+    int dtype;    // IWPP_U8 / U16 / I32, or -1 for a mixed batch
+    int conn;     // 4 / 8, or -1 for a mixed batch
+    int pxclass;  // floor(log2(total pixels))
+    int batch;    // 0 single image, 1 several
+    bool operator<(const TuneKey& o) const;
+};
+
+struct TuneEntry {
+    int tile_rows;   // 32 / 64
+    int solver;      // 0 / 1 / 2
+    int init_passes;
+    int queue_mult;  // queue capacity in tiles per tile of the job; 0 = the variant's default
+};
+
+int resolve_queue_variant(int variant);  // iwpp_api.cu: IWPP_QUEUE_DEFAULT -> the variant used
+TuneKey tune_key(int variant, const int* dtypes, const int* conns, const long long* pixels, int n);
+bool tune_lookup(const TuneKey& k, TuneEntry* e);
+void tune_store(const TuneKey& k, const TuneEntry& e);
+
+}  // namespace iwpp

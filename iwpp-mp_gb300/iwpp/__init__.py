@@ -95,6 +95,11 @@ class ServerStats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class TuneResult(ctypes.Structure):
+    _fields_ = [("best", Config), ("best_ms", ctypes.c_double), ("default_ms", ctypes.c_double),
+                ("candidates", ctypes.c_int), ("reserved", ctypes.c_int)]
+
+
 # Every symbol include/iwpp.h declares, with its ctypes signature.
 _SIGS = {
     "iwpp_status_string": (ctypes.c_char_p, [ctypes.c_int]),
@@ -131,6 +136,14 @@ _SIGS = {
     "iwpp_reconstruct_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
                                                 ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_void_p]),
+    "iwpp_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Image), ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(TuneResult)]),
+    "iwpp_tune_save": (ctypes.c_int, [ctypes.c_char_p]),
+    "iwpp_tune_load": (ctypes.c_int, [ctypes.c_char_p]),
+    "iwpp_tune_clear": (ctypes.c_int, []),
+    "iwpp_tune_entries": (ctypes.c_int, []),
+    "iwpp_tune_lookup": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_longlong, ctypes.c_int,
+                                        ctypes.POINTER(Config)]),
     "iwpp_server_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
                                           ctypes.POINTER(ServerConfig)]),
     "iwpp_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -312,6 +325,59 @@ def reconstruct_batch(pairs: Sequence, connectivity=None, variant="default", con
         raise IwppError(st, "iwpp_reconstruct_batch")
     stats.status = st
     return stats
+
+
+def autotune(pairs: Sequence, variant="default", repeats: int = 0, handle: Optional["Handle"] = None,
+             stream=None) -> dict:
+    """iwpp_autotune over (marker, mask[, connectivity]) pairs: times the
+    candidate configurations, records the fastest in the tuning table and
+    leaves the markers reconstructed.  Returns the winner and its timings."""
+    lib = load()
+    arr = (Image * max(len(pairs), 1))()
+    for i, p in enumerate(pairs):
+        m, k = p[0], p[1]
+        conn = p[2] if len(p) > 2 else 8
+        _check_cuda(m, "marker")
+        _check_cuda(k, "mask")
+        arr[i] = Image(m.data_ptr(), k.data_ptr(), _pitch(m), _pitch(k), m.shape[1], m.shape[0], dtype_code(m), conn)
+    res = TuneResult()
+    h = handle or Handle(pairs[0][0].device.index or 0)
+    st = lib.iwpp_autotune(h.ptr, arr, len(pairs), _variant(variant), repeats, _stream_ptr(stream), ctypes.byref(res))
+    if st != 0:
+        raise IwppError(st, "iwpp_autotune")
+    b = res.best
+    return {"tile_rows": b.tile_rows, "solver": b.solver, "init_passes": b.init_passes,
+            "queue_capacity": b.queue_capacity, "best_ms": res.best_ms, "default_ms": res.default_ms,
+            "candidates": res.candidates}
+
+
+def tune_save(path: str) -> None:
+    st = load().iwpp_tune_save(os.fsencode(path))
+    if st != 0:
+        raise IwppError(st, "iwpp_tune_save")
+
+
+def tune_load(path: str) -> None:
+    st = load().iwpp_tune_load(os.fsencode(path))
+    if st != 0:
+        raise IwppError(st, "iwpp_tune_load")
+
+
+def tune_clear() -> None:
+    load().iwpp_tune_clear()
+
+
+def tune_entries() -> int:
+    return int(load().iwpp_tune_entries())
+
+
+def tune_lookup(variant, dtype: int, connectivity: int, pixels: int, batch: bool = False) -> Optional[dict]:
+    c = Config()
+    st = load().iwpp_tune_lookup(_variant(variant), dtype, connectivity, pixels, 1 if batch else 0, ctypes.byref(c))
+    if st != 0:
+        return None
+    return {"tile_rows": c.tile_rows, "solver": c.solver, "init_passes": c.init_passes,
+            "queue_capacity": c.queue_capacity}
 
 
 class Plan:
