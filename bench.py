@@ -66,6 +66,25 @@ def _dist_env():
     return world, rank, local
 
 
+def max_over_ranks(x: float, device=None) -> float:
+    """The largest x over all ranks of the default process group (x itself
+    without one): the job's time is its slowest replica's."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gpx(world: int, px_per_rank_step: int, steps: int, elapsed_ms: float) -> float:
+    """Replicas: every rank processes its own copy of the workload, so the
+    job processed world x the pixels of one rank in the slowest rank's time."""
+    return world * px_per_rank_step * steps / (elapsed_ms / 1e3) / 1e9
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
 
@@ -496,11 +515,9 @@ def run_ours(args):
     elapsed_ms = t_start.elapsed_time(t_end)
     recon_ms = [a.elapsed_time(b) for row in ev for (a, b) in row]
     if world > 1:
-        t = torch.tensor([elapsed_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+        elapsed_ms = max_over_ranks(elapsed_ms, dev)
         torch.distributed.barrier()
-    value = world * px_step * args.steps / (elapsed_ms / 1e3) / 1e9
+    value = whole_job_gpx(world, px_step, args.steps, elapsed_ms)
 
     # ---- end to end: host buffers, reference-facing synchronous call
     e2e = None
