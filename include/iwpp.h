@@ -144,6 +144,25 @@ IWPP_API int iwpp_plan_launch(iwpp_plan p, void *stream);
 IWPP_API int iwpp_plan_sync(iwpp_plan p, iwpp_stats *stats);
 IWPP_API int iwpp_plan_destroy(iwpp_plan p);
 
+/* ---- queue self-test ------------------------------------------------------ */
+/* The counterpart of the reference's queue test (IWPP MP DQ/src/
+ * globalQueue.cu:161-253, testGlobalQueue / verifyQueue / compareKernel):
+ * every warp of a full grid inserts every id of a grid_side x grid_side tile
+ * grid `copies` times at once through the variant's own insertion path
+ * (mutex stack, write-queue reservations, unique dedup through the tile
+ * state word, async ring); the queue is then counted per id on the device.
+ * Each id must appear `copies` times (once for the unique queue).  Returns
+ * the device status of the run; `out` says whether the counts were right. */
+typedef struct iwpp_queue_test_result {
+    long long entries;     /* entries found in the queue */
+    long long expected;    /* entries the inserts should leave */
+    long long mismatched;  /* ids seen a wrong number of times */
+    long long first_bad;   /* the smallest such id, -1 if none */
+    int status;            /* device status of the run */
+    int variant;           /* queue variant tested */
+} iwpp_queue_test_result;
+IWPP_API int iwpp_queue_selftest(int device, int variant, int grid_side, int copies, iwpp_queue_test_result *out);
+
 /* ---- autotuner ------------------------------------------------------------ */
 /* No counterpart in the reference (its tile size, queue sizes and number of
  * initial passes are compile-time constants, IWPP MP/include/
@@ -180,6 +199,15 @@ IWPP_API int iwpp_tune_lookup(int variant, int dtype, int connectivity, long lon
  *      IWPP MP/src/MorphologicalReconstruction.cu:827-836) ----------------- */
 IWPP_API int iwpp_clip(void *marker, const void *mask, size_t pitch_marker, size_t pitch_mask, int width,
                        int height, int dtype, void *stream);
+
+/* ---- result check ------------------------------------------------------------ */
+/* Counts the pixels c of `result` that a neighbour p could still raise,
+ * min(result[p], mask[c]) > result[c]: zero for every reconstruction.  A
+ * size-independent check for images too large to compare on the CPU.
+ * Synchronous on `stream`; any pixel-aligned pitch. */
+IWPP_API int iwpp_fixed_point_violations(const void *result, const void *mask, size_t pitch_result,
+                                         size_t pitch_mask, int width, int height, int dtype, int connectivity,
+                                         void *stream, unsigned long long *count);
 
 /* ---- whole-image raster / anti-raster sweeps (the reference's
  *      *PropagationEntireImage kernels, MR.cu:547-753, and iRec1D*,

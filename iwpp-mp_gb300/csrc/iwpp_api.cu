@@ -882,6 +882,62 @@ int iwpp_plan_destroy(iwpp_plan p) {
     return IWPP_OK;
 }
 
+int iwpp_queue_selftest(int device, int variant, int grid_side, int copies, iwpp_queue_test_result* out) {
+    if (grid_side < 1 || grid_side > 4096 || copies < 1 || copies > 16) return set_last(IWPP_ERR_INVALID);
+    int rc = check_device(device);
+    if (rc != IWPP_OK) return set_last(rc);
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(device);
+    const int v = resolve_variant(variant);
+    const long long G = (long long)grid_side * grid_side;
+    const long long cap = v == IWPP_QUEUE_UNIQUE ? G : G * copies;
+    const size_t off_state = align_up(sizeof(Ctrl), 256);
+    const size_t off_q0 = align_up(off_state + (size_t)G * 4u, 256);
+    const size_t off_q1 = align_up(off_q0 + (size_t)cap * 4u, 256);
+    const size_t off_hist = align_up(off_q1 + (size_t)cap * 4u, 256);
+    const size_t off_out = align_up(off_hist + (size_t)G * 4u, 256);
+    const size_t total = off_out + 3 * sizeof(unsigned long long);
+    char* base = nullptr;
+    cudaStream_t s = nullptr;
+    cudaError_t e = cudaMalloc(&base, total);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    unsigned long long res[3] = {0ull, 0ull, ~0ull};
+    Ctrl ctrl;
+    std::memset(&ctrl, 0, sizeof(ctrl));
+    if (e == cudaSuccess) {
+        EngineArgs a{};
+        a.G = (unsigned)G;
+        a.state = reinterpret_cast<unsigned*>(base + off_state);
+        a.q0 = reinterpret_cast<unsigned*>(base + off_q0);
+        a.q1 = reinterpret_cast<unsigned*>(base + off_q1);
+        a.cap = (unsigned)cap;
+        a.ctrl = reinterpret_cast<Ctrl*>(base);
+        a.timeout_ns = 10ll * 1000000000ll;
+        a.max_restarts = 0;
+        e = queue_selftest(a, v, copies, reinterpret_cast<unsigned*>(base + off_hist),
+                           reinterpret_cast<unsigned long long*>(base + off_out), device, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(res, base + off_out, sizeof(res), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&ctrl, base, sizeof(Ctrl), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
+    rc = cuda_status(e);
+    if (rc == IWPP_OK && ctrl.error == DEV_ERR_TIMEOUT) rc = IWPP_ERR_TIMEOUT;
+    if (rc == IWPP_OK && ctrl.overflow != 0u) rc = IWPP_ERR_OVERFLOW;
+    if (out) {
+        out->entries = (long long)res[0];
+        out->expected = v == IWPP_QUEUE_UNIQUE ? G : G * copies;
+        out->mismatched = (long long)res[1];
+        out->first_bad = res[1] ? (long long)res[2] : -1;
+        out->status = rc;
+        out->variant = v;
+    }
+    if (s) cudaStreamDestroy(s);
+    if (base) cudaFree(base);
+    cudaSetDevice(prev);
+    return set_last(rc);
+}
+
 int iwpp_autotune(iwpp_handle h, const iwpp_image* images, int n, int variant, int repeats, void* stream,
                   iwpp_tune_result* out) {
     if (!h || n <= 0 || !images || repeats < 0 || repeats > 50) return set_last(IWPP_ERR_INVALID);
@@ -1061,6 +1117,35 @@ int iwpp_clip(void* marker, const void* mask, size_t pitch_marker, size_t pitch_
         return set_last(rc == IWPP_OK ? rc2 : rc);
     }
     return set_last(cuda_status(launch_clip(d, static_cast<cudaStream_t>(stream))));
+}
+
+int iwpp_fixed_point_violations(const void* result, const void* mask, size_t pitch_result, size_t pitch_mask,
+                                int width, int height, int dtype, int connectivity, void* stream,
+                                unsigned long long* count) {
+    if (!count) return set_last(IWPP_ERR_INVALID);
+    *count = 0ull;
+    int rc = check_image(result, mask, pitch_result, pitch_mask, width, height, dtype, connectivity);
+    if (rc != IWPP_OK || width == 0 || height == 0) return set_last(rc);
+    ImgDesc d{};
+    d.marker = static_cast<unsigned char*>(const_cast<void*>(result));
+    d.mask = static_cast<const unsigned char*>(mask);
+    d.pitch_m = (long long)pitch_result;
+    d.pitch_k = (long long)pitch_mask;
+    d.W = width;
+    d.H = height;
+    d.dtype = dtype;
+    d.conn = connectivity;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned long long* dc = nullptr;
+    cudaError_t e = cudaMallocAsync(&dc, sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dc, 0, sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = launch_fixed_point_check(d, dc, s);
+    unsigned long long host = 0ull;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&host, dc, sizeof(host), cudaMemcpyDeviceToHost, s);
+    if (dc) cudaFreeAsync(dc, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    *count = host;
+    return set_last(cuda_status(e));
 }
 
 int iwpp_sweep(void* marker, const void* mask, size_t pitch_marker, size_t pitch_mask, int width, int height,

@@ -620,6 +620,105 @@ __global__ void engine_init_kernel(EngineArgs a, int variant) {
     }
 }
 
+// ------------------------------------------------------- queue self-test
+// The counterpart of the reference's queue test (IWPP MP DQ/src/
+// globalQueue.cu:161-253: fill a 128 x 128 tile-id queue several times, read
+// it back, check every id's count): all warps insert every tile id `copies`
+// times at once through the variant's own insertion path (push_entries:
+// mutex stack, warp-aggregated write-queue reservations, async ring; the
+// unique queue deduplicates through the tile state word as notify does),
+// then the queue's contents are counted per id.
+struct QueueTest {
+    unsigned* hist;          // G counters
+    unsigned long long* out;  // [0] entries found, [1] ids with a wrong count, [2] smallest such id
+};
+
+__global__ void queue_test_init_kernel(EngineArgs a, QueueTest t) {
+    const unsigned stride = gridDim.x * blockDim.x;
+    for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < a.G; g += stride) {
+        a.state[g] = 0u;
+        t.hist[g] = 0u;
+    }
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < a.cap; i += stride) {
+        a.q0[i] = 0u;
+        a.q1[i] = 0u;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        Ctrl* c = a.ctrl;
+        c->wn = 0u;
+        c->overflow = 0u;
+        c->error = 0u;
+        c->lock = 0;
+        c->top = 0;
+        c->pending = 0;
+        c->atail = a.G;  // ring positions below G are the (absent) initial tiles
+        t.out[0] = 0ull;
+        t.out[1] = 0ull;
+        t.out[2] = ~0ull;
+    }
+}
+
+template <int VAR>
+__global__ void queue_test_insert_kernel(EngineArgs a, int copies) {
+    const int lane = threadIdx.x & 31;
+    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
+    const unsigned total = a.G * (unsigned)copies;
+    WarpCounters cnt;
+    for (unsigned base = warp * 32u; base < total; base += nwarps * 32u) {
+        const unsigned idx = base + (unsigned)lane;
+        bool want = idx < total;
+        const unsigned g = want ? idx % a.G : 0u;
+        if (VAR == VAR_UNIQUE && want) want = (atomicOr(&a.state[g], ST_DIRTY) & ST_DIRTY) == 0u;
+        push_entries<VAR>(a, want, g, lane, a.q1, cnt);
+        if (ld_volatile(&a.ctrl->error) != 0u) return;
+    }
+}
+
+__global__ void queue_test_count_kernel(EngineArgs a, int variant, QueueTest t) {
+    const Ctrl* c = a.ctrl;
+    unsigned n;
+    if (variant == VAR_MUTEX) n = (unsigned)c->top;
+    else if (variant == VAR_ASYNC) n = c->atail - a.G;
+    else n = c->wn;
+    if (n > a.cap) n = a.cap;
+    if (blockIdx.x == 0 && threadIdx.x == 0) t.out[0] = n;
+    const unsigned stride = gridDim.x * blockDim.x;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        unsigned e = variant == VAR_MUTEX ? a.q0[i] : variant == VAR_ASYNC ? a.q0[i] - 1u : a.q1[i];
+        if (e < a.G) atomicAdd(&t.hist[e], 1u);
+    }
+}
+
+__global__ void queue_test_check_kernel(EngineArgs a, QueueTest t, unsigned expect) {
+    const unsigned stride = gridDim.x * blockDim.x;
+    for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < a.G; g += stride) {
+        if (t.hist[g] != expect) {
+            atomicAdd(&t.out[1], 1ull);
+            atomicMin(&t.out[2], (unsigned long long)g);
+        }
+    }
+}
+
+cudaError_t queue_selftest(const EngineArgs& a, int variant, int copies, unsigned* hist, unsigned long long* out,
+                           int device, cudaStream_t s) {
+    int sms = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) return e;
+    QueueTest t{hist, out};
+    const unsigned blocks = (unsigned)sms * 4u;
+    queue_test_init_kernel<<<blocks, 256, 0, s>>>(a, t);
+    switch (variant) {
+        case VAR_MUTEX: queue_test_insert_kernel<VAR_MUTEX><<<blocks, 128, 0, s>>>(a, copies); break;
+        case VAR_DOUBLE: queue_test_insert_kernel<VAR_DOUBLE><<<blocks, 128, 0, s>>>(a, copies); break;
+        case VAR_UNIQUE: queue_test_insert_kernel<VAR_UNIQUE><<<blocks, 128, 0, s>>>(a, copies); break;
+        default: queue_test_insert_kernel<VAR_ASYNC><<<blocks, 128, 0, s>>>(a, copies); break;
+    }
+    queue_test_count_kernel<<<blocks, 256, 0, s>>>(a, variant, t);
+    queue_test_check_kernel<<<blocks, 256, 0, s>>>(a, t, variant == VAR_UNIQUE ? 1u : (unsigned)copies);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------ host side
 template <int VAR, int TH>
 static void* kernel_ptr() {

@@ -93,5 +93,13 @@ cudaError_t engine_prepare(int variant, int tile_rows, int device, LaunchInfo* l
 cudaError_t engine_launch_init(const EngineArgs& a, int variant, cudaStream_t s);
 cudaError_t engine_launch(const EngineArgs& a, int variant, int tile_rows, int grid, cudaStream_t s);
 cudaError_t launch_clip(const ImgDesc& d, cudaStream_t s);
+// Adds to *count the pixels of d.marker that a neighbour could still raise.
+cudaError_t launch_fixed_point_check(const ImgDesc& d, unsigned long long* count, cudaStream_t s);
+// Queue self-test on workspace `a` (state G words, q0 / q1 cap entries each):
+// insert every tile id `copies` times through the variant's insertion path,
+// count the queue's contents into hist (G words); out[0] entries found,
+// out[1] ids with a wrong count, out[2] the smallest such id.
+cudaError_t queue_selftest(const EngineArgs& a, int variant, int copies, unsigned* hist, unsigned long long* out,
+                           int device, cudaStream_t s);
 cudaError_t launch_sweep(const ImgDesc& d, int direction, cudaStream_t s);
 }  // namespace iwpp

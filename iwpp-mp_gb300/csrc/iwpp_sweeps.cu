@@ -61,6 +61,41 @@ __global__ void clip_kernel(ImgDesc d) {
     }
 }
 
+// ------------------------------------------------------ fixed-point check
+// Counts the pixels c that a neighbour p could still raise:
+// min(m[p], mask[c]) > m[c].  Zero on every reconstruction (it is a fixed
+// point of the propagation rule, MR.cu:43-44); a size-independent check for
+// images too large for a CPU comparison.
+template <int DT>
+__global__ void fixed_point_kernel(ImgDesc d, unsigned long long* count) {
+    using P = Px<DT>;
+    const long long total = (long long)d.W * d.H;
+    unsigned long long mine = 0ull;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int y = (int)(i / d.W), x = (int)(i - (long long)y * d.W);
+        const unsigned char* mrow = d.marker + (size_t)y * d.pitch_m;
+        const uint32_t m = P::ld_px(mrow + (size_t)x * P::BPP);
+        const uint32_t k = P::ld_px(d.mask + (size_t)y * d.pitch_k + (size_t)x * P::BPP);
+        if (!P::gt(k, m)) continue;  // m == mask[c] (or above it): nothing can raise it
+        uint32_t best = P::MINPX;
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int yy = y + dy;
+            if (yy < 0 || yy >= d.H) continue;
+            const unsigned char* row = d.marker + (size_t)yy * d.pitch_m;
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int xx = x + dx;
+                if ((dx == 0 && dy == 0) || xx < 0 || xx >= d.W) continue;
+                if (d.conn == 4 && dx != 0 && dy != 0) continue;
+                best = P::mx(best, P::ld_px(row + (size_t)xx * P::BPP));
+            }
+        }
+        if (P::gt(P::mn(best, k), m)) ++mine;
+    }
+    const unsigned long long warp_sum = __reduce_add_sync(0xffffffffu, (unsigned)mine);
+    if ((threadIdx.x & 31) == 0 && warp_sum) atomicAdd(count, warp_sum);
+}
+
 // --------------------------------------------------------------- X sweeps
 template <int DT, bool FWD>
 __global__ void sweep_x_kernel(ImgDesc d) {
@@ -138,6 +173,19 @@ static unsigned blocks_for(long long threads, int block) {
     if (b < 1) b = 1;
     if (b > (1ll << 30)) b = 1ll << 30;
     return (unsigned)b;
+}
+
+cudaError_t launch_fixed_point_check(const ImgDesc& d, unsigned long long* count, cudaStream_t s) {
+    if (d.W == 0 || d.H == 0) return cudaSuccess;
+    unsigned blocks = blocks_for((long long)d.W * d.H, 256);
+    if (blocks > 152u * 16u) blocks = 152u * 16u;
+    if (d.dtype == DT_U8)
+        fixed_point_kernel<DT_U8><<<blocks, 256, 0, s>>>(d, count);
+    else if (d.dtype == DT_U16)
+        fixed_point_kernel<DT_U16><<<blocks, 256, 0, s>>>(d, count);
+    else
+        fixed_point_kernel<DT_I32><<<blocks, 256, 0, s>>>(d, count);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_clip(const ImgDesc& d, cudaStream_t s) {

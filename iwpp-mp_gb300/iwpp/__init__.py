@@ -100,6 +100,14 @@ class TuneResult(ctypes.Structure):
                 ("candidates", ctypes.c_int), ("reserved", ctypes.c_int)]
 
 
+class QueueTestResult(ctypes.Structure):
+    _fields_ = [("entries", ctypes.c_longlong), ("expected", ctypes.c_longlong), ("mismatched", ctypes.c_longlong),
+                ("first_bad", ctypes.c_longlong), ("status", ctypes.c_int), ("variant", ctypes.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # Every symbol include/iwpp.h declares, with its ctypes signature.
 _SIGS = {
     "iwpp_status_string": (ctypes.c_char_p, [ctypes.c_int]),
@@ -136,6 +144,12 @@ _SIGS = {
     "iwpp_reconstruct_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
                                                 ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_void_p]),
+    "iwpp_fixed_point_violations": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                   ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                   ctypes.c_int, ctypes.c_void_p,
+                                                   ctypes.POINTER(ctypes.c_ulonglong)]),
+    "iwpp_queue_selftest": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.POINTER(QueueTestResult)]),
     "iwpp_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Image), ctypes.c_int, ctypes.c_int,
                                      ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(TuneResult)]),
     "iwpp_tune_save": (ctypes.c_int, [ctypes.c_char_p]),
@@ -349,6 +363,27 @@ def autotune(pairs: Sequence, variant="default", repeats: int = 0, handle: Optio
     return {"tile_rows": b.tile_rows, "solver": b.solver, "init_passes": b.init_passes,
             "queue_capacity": b.queue_capacity, "best_ms": res.best_ms, "default_ms": res.default_ms,
             "candidates": res.candidates}
+
+
+def fixed_point_violations(result, mask, connectivity: int = 8, stream=None) -> int:
+    """Pixels of `result` (device tensor) that a neighbour could still raise."""
+    n = ctypes.c_ulonglong()
+    h, w = result.shape
+    st = load().iwpp_fixed_point_violations(result.data_ptr(), mask.data_ptr(), _pitch(result), _pitch(mask), w, h,
+                                            dtype_code(result), connectivity, _stream_ptr(stream), ctypes.byref(n))
+    if st != 0:
+        raise IwppError(st, "iwpp_fixed_point_violations")
+    return int(n.value)
+
+
+def queue_selftest(variant="default", grid_side: int = 128, copies: int = 2, device: int = 0) -> dict:
+    """iwpp_queue_selftest: the reference's fill / read-back queue check on
+    this library's queues.  Raises if the run itself failed."""
+    r = QueueTestResult()
+    st = load().iwpp_queue_selftest(device, _variant(variant), grid_side, copies, ctypes.byref(r))
+    if st != 0:
+        raise IwppError(st, "iwpp_queue_selftest")
+    return r.as_dict()
 
 
 def tune_save(path: str) -> None:

@@ -2,6 +2,8 @@
 
 * ``libiwpp.so``        -- CUDA kernels + C ABI (``include/iwpp.h``), sm_103a only.
 * ``libiwpp_synth.so``  -- deterministic synthetic inputs (host C).
+* ``iwpp_cli``          -- command-line front end with the reference's
+  arguments (PGM / TIFF / raw I/O), linked against ``libiwpp.so``.
 
 Object files are compiled in parallel; a library is rebuilt when any of its
 sources is newer than it.
@@ -28,6 +30,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvi
 
 LIBIWPP = os.path.join(LIB_DIR, "libiwpp.so")
 LIBSYNTH = os.path.join(LIB_DIR, "libiwpp_synth.so")
+CLI = os.path.join(LIB_DIR, "iwpp_cli")
 
 
 def _nvcc() -> str:
@@ -83,12 +86,22 @@ def build_synth(force: bool = False) -> str:
     return LIBSYNTH
 
 
+def build_cli(force: bool = False) -> str:
+    """Needs libiwpp.so; found next to the executable at run time."""
+    src = os.path.join(SRC_DIR, "iwpp_cli.cpp")
+    if force or _stale(CLI, [src, LIBIWPP, os.path.join(INCLUDE_DIR, "iwpp.h")]):
+        _run([_nvcc(), "-O2", "-std=c++17", "-I" + INCLUDE_DIR, "-o", CLI, src, "-L" + LIB_DIR, "-liwpp",
+              "-Xlinker", "-rpath,$ORIGIN"])
+    return CLI
+
+
 def build_all(force: bool = False) -> None:
     with ThreadPoolExecutor(max_workers=2) as ex:
         f1 = ex.submit(build_iwpp, force)
         f2 = ex.submit(build_synth, force)
         f1.result()
         f2.result()
+    build_cli(force)
 
 
 if __name__ == "__main__":

@@ -117,3 +117,21 @@ def test_server_host_side_checks():
     except ImportError:
         pass
     assert lib.iwpp_server_create(ctypes.byref(srv), 0, None) == 6
+
+
+def test_selftest_and_checker_host_side():
+    lib = iwpp.load()
+    r = iwpp.QueueTestResult()
+    assert lib.iwpp_queue_selftest(0, -1, 0, 2, ctypes.byref(r)) == 1
+    assert lib.iwpp_queue_selftest(0, -1, 128, 99, ctypes.byref(r)) == 1
+    n = ctypes.c_ulonglong()
+    assert lib.iwpp_fixed_point_violations(16, 16, 64, 64, 64, 64, 0, 8, None, None) == 1
+    assert lib.iwpp_fixed_point_violations(16, 16, 32, 64, 64, 64, 0, 8, None, ctypes.byref(n)) == 1
+    assert lib.iwpp_fixed_point_violations(None, None, 0, 0, 0, 0, 0, 8, None, ctypes.byref(n)) == 0
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return
+    except ImportError:
+        pass
+    assert lib.iwpp_queue_selftest(0, -1, 128, 2, ctypes.byref(r)) == 6
