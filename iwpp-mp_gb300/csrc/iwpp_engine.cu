@@ -48,27 +48,44 @@ struct WarpCounters {
 };
 
 // ---------------------------------------------------------------- mutex
-// Bounded spin on the global mutex (IWPP MP/src/globalQueue.cu:35, :114 spin
-// without a bound; here a wall-clock bound ends in DEV_ERR_TIMEOUT).
-__device__ bool mutex_lock(const EngineArgs& a) {
-    const long long t0 = globaltimer_ns();
-    unsigned ns = 32;
-    while (atomicCAS(&a.ctrl->lock, 0, 1) != 0) {
-        __nanosleep(ns);
-        if (ns < 1024) ns <<= 1;
-        if (ld_volatile(&a.ctrl->error) != 0u) return false;
-        if (globaltimer_ns() - t0 > a.timeout_ns) {
-            set_error(a.ctrl, DEV_ERR_TIMEOUT);
-            return false;
-        }
-    }
-    __threadfence();
-    return true;
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-__device__ __forceinline__ void mutex_unlock(const EngineArgs& a) {
-    __threadfence();
-    atomicExch(&a.ctrl->lock, 0);
+// The global mutex (IWPP MP/src/globalQueue.cu:35, :114, a CAS spin without
+// a bound) as a ticket lock: one atomic per acquisition instead of a CAS
+// storm from every waiting warp, hand-over in arrival order, acquire /
+// release ordering instead of full fences; waiters poll the ticket being
+// served with a back-off proportional to their place in line, and a
+// wall-clock bound ends in DEV_ERR_TIMEOUT.  A waiter that gives up leaves
+// the error flag set, which ends every other waiter too.
+__device__ bool mutex_lock(const EngineArgs& a, unsigned* ticket) {
+    const unsigned t = atomicAdd(&a.ctrl->lock_next, 1u);
+    *ticket = t;
+    const long long t0 = globaltimer_ns();
+    unsigned spins = 0;
+    for (;;) {
+        const unsigned s = ld_acquire(&a.ctrl->lock_serving);
+        if (s == t) return true;
+        const unsigned place = t - s;
+        __nanosleep(32u * (place < 32u ? place : 32u));
+        if ((++spins & 15u) == 0u) {
+            if (ld_volatile(&a.ctrl->error) != 0u) return false;
+            if (globaltimer_ns() - t0 > a.timeout_ns) {
+                set_error(a.ctrl, DEV_ERR_TIMEOUT);
+                return false;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void mutex_unlock(const EngineArgs& a, unsigned ticket) {
+    st_release(&a.ctrl->lock_serving, ticket + 1u);
 }
 
 // ------------------------------------------------------------------ push
@@ -87,26 +104,29 @@ __device__ void push_entries(const EngineArgs& a, bool want, unsigned gn, int la
     const int rank = __popc(ballot & ((1u << lane) - 1u));
     if (VAR == VAR_MUTEX) {
         int base = -1;
+        unsigned ticket = 0u;
         if (lane == 0) {
-            if (mutex_lock(a)) {
+            if (mutex_lock(a, &ticket)) {
                 const int top = ld_volatile(&a.ctrl->top);
                 if ((unsigned)top + (unsigned)n <= a.cap) {
                     base = top;
                     atomicAdd(&a.ctrl->pending, n);  // before the entries can be taken
                 } else {
                     atomicExch(&a.ctrl->overflow, 1u);
-                    mutex_unlock(a);
+                    mutex_unlock(a, ticket);
                 }
             }
         }
         base = __shfl_sync(FULL, base, 0);
         if (base < 0) return;
-        if (want) a.q0[base + rank] = gn;
+        if (want) {
+            a.q0[base + rank] = gn;
+            __threadfence();  // the entry before the release that publishes it
+        }
         __syncwarp();
         if (lane == 0) {
-            __threadfence();
             *(volatile int*)&a.ctrl->top = base + n;
-            mutex_unlock(a);
+            mutex_unlock(a, ticket);
         }
     } else if (VAR == VAR_ASYNC) {
         // positions [base, base + n) of the ring; `pending` first, so the job
@@ -153,7 +173,7 @@ __device__ void push_entries(const EngineArgs& a, bool want, unsigned gn, int la
 template <int VAR>
 __device__ unsigned notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty, unsigned nb, int lane, unsigned* wq,
                            WarpCounters& cnt, bool keep_one = true) {
-    bool want = false;
+    bool want = false, fresh = false;
     unsigned gn = 0u;
     if (lane < 8 && ((nb >> lane) & 1u)) {
         const int nx = tx + kNbDx[lane], ny = ty + kNbDy[lane];
@@ -161,12 +181,15 @@ __device__ unsigned notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty
             gn = (unsigned)d.tile_base + (unsigned)(ny * d.tiles_x + nx);
             const unsigned old =
                 atomicOr(&a.state[gn], ST_DIRTY | (1u << (ST_SIDE_SHIFT + (unsigned)kNbOpposite[lane])));
-            want = (VAR == VAR_UNIQUE || VAR == VAR_ASYNC) ? (old & (ST_DIRTY | ST_ACTIVE)) == 0u : true;
+            fresh = (old & (ST_DIRTY | ST_ACTIVE)) == 0u;
+            want = (VAR == VAR_UNIQUE || VAR == VAR_ASYNC) ? fresh : true;
         }
     }
     unsigned cont = ~0u;
-    if (VAR == VAR_ASYNC && keep_one) {
-        const unsigned ballot = __ballot_sync(FULL, want);
+    if ((VAR == VAR_ASYNC || VAR == VAR_MUTEX) && keep_one) {
+        // one newly dirty neighbour is kept by this warp (its next visit)
+        // instead of going through the queue
+        const unsigned ballot = __ballot_sync(FULL, want && fresh);
         if (ballot != 0u) {
             const int leader = __ffs(ballot) - 1;
             cont = __shfl_sync(FULL, gn, leader);
@@ -291,23 +314,38 @@ __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
     for (;;) {
         int n = 0, base = 0, verdict = 0;  // verdict: 0 work/retry, 1 exit, 2 refill
         const long long qr0 = clock64();
-        // Test before test-and-set: an idle warp looks at the stack without
-        // the lock and takes it only when there is something to take or the
-        // job looks finished, so idle pollers never starve a warp that
-        // inserts.
+        // Look before queueing for the lock: an idle warp takes a ticket only
+        // while the stack holds more entries than there are warps in line
+        // (a ticket lock serves in arrival order, so idle warps queued for an
+        // empty stack would delay every warp that inserts), or when the job
+        // looks finished but an overflow needs the refill.  A finished job
+        // (no entry in the stack or in flight, no overflow) is left without
+        // the lock.
         if (ld_volatile(&a.ctrl->error) != 0u) return;
-        bool try_lock = true;
-        if (lane == 0)
-            try_lock = ld_volatile(&a.ctrl->top) > 0 || ld_volatile(&a.ctrl->pending) == 0 ||
-                       ld_volatile(&a.ctrl->error) != 0u;
-        try_lock = __shfl_sync(FULL, try_lock ? 1 : 0, 0) != 0;
+        int look = 0;  // 0 back off, 1 take a ticket, 2 finished
+        if (lane == 0) {
+            const int top = ld_volatile(&a.ctrl->top);
+            const int pend = ld_volatile(&a.ctrl->pending);
+            const unsigned line = ld_volatile(&a.ctrl->lock_next) - ld_volatile(&a.ctrl->lock_serving);
+            if (pend == 0 && top == 0 && ld_volatile(&a.ctrl->overflow) == 0u)
+                look = 2;
+            else if (top > (int)line || pend == 0)
+                look = 1;
+        }
+        look = __shfl_sync(FULL, look, 0);
+        if (look == 2) return;
+        const bool try_lock = look == 1;
+        unsigned ticket = 0u;
         if (lane == 0 && try_lock) {
-            if (!mutex_lock(a)) {
+            if (!mutex_lock(a, &ticket)) {
                 verdict = 1;
             } else {
                 const int top = ld_volatile(&a.ctrl->top);
                 if (top > 0) {
-                    n = top < kMutexBatch ? top : kMutexBatch;
+                    // a share that leaves entries for other warps while the
+                    // stack is short, up to kMutexBatch while it is long
+                    n = top >> 8;
+                    n = n < 1 ? 1 : n > kMutexBatch ? kMutexBatch : n;
                     base = top - n;
                 } else if (ld_volatile(&a.ctrl->pending) == 0) {
                     if (ld_volatile(&a.ctrl->overflow) != 0u) {
@@ -321,7 +359,7 @@ __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
                         verdict = 1;
                     }
                 }
-                if (n == 0 && verdict != 2) mutex_unlock(a);
+                if (n == 0 && verdict != 2) mutex_unlock(a, ticket);
             }
         }
         n = __shfl_sync(FULL, n, 0);
@@ -339,7 +377,7 @@ __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
                 atomicAdd(&a.ctrl->restarts, 1u);
                 __threadfence();
                 *(volatile int*)&a.ctrl->top = cnt_all;
-                mutex_unlock(a);
+                mutex_unlock(a, ticket);
             }
             __syncwarp();
             continue;
@@ -370,11 +408,17 @@ __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
         __syncwarp();
         if (lane == 0) {
             *(volatile int*)&a.ctrl->top = base;
-            mutex_unlock(a);
+            mutex_unlock(a, ticket);
         }
         for (int j = 0; j < n; ++j) {
-            const unsigned g = __shfl_sync(FULL, mine, j);
-            const bool ok = process_entry<VAR_MUTEX, TH>(a, g, sm, lane, nullptr, cnt, phase);
+            unsigned g = __shfl_sync(FULL, mine, j);
+            bool ok = true;
+            for (;;) {  // the entry, then the newly dirty neighbours it leaves behind
+                unsigned nxt = ~0u;
+                ok = process_entry<VAR_MUTEX, TH>(a, g, sm, lane, nullptr, cnt, phase, &nxt);
+                if (!ok || nxt == ~0u) break;
+                g = nxt;
+            }
             if (!ok) return;
             if (lane == 0) {
                 __threadfence();
@@ -605,7 +649,8 @@ __global__ void engine_init_kernel(EngineArgs a, int variant) {
         c->bar_count = 0u;
         c->bar_gen = 0u;
         c->error = 0u;
-        c->lock = 0;
+        c->lock_next = 0u;
+        c->lock_serving = 0u;
         c->top = (int)(a.G < a.cap ? a.G : a.cap);
         c->pending = (int)(a.G < a.cap ? a.G : a.cap);
         c->progress = 0u;
@@ -648,7 +693,8 @@ __global__ void queue_test_init_kernel(EngineArgs a, QueueTest t) {
         c->wn = 0u;
         c->overflow = 0u;
         c->error = 0u;
-        c->lock = 0;
+        c->lock_next = 0u;
+        c->lock_serving = 0u;
         c->top = 0;
         c->pending = 0;
         c->atail = a.G;  // ring positions below G are the (absent) initial tiles

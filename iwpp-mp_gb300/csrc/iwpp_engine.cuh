@@ -53,7 +53,8 @@ struct Ctrl {
     unsigned bar_count;
     unsigned bar_gen;
     unsigned error;
-    int lock;           // mutex stack
+    unsigned lock_next;     // mutex stack: ticket lock (next ticket, ticket being served)
+    unsigned lock_serving;
     int top;
     int pending;        // mutex: entries in the stack or taken and unfinished
     unsigned progress;  // finished entries (for the no-progress timeout)

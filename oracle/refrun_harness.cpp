@@ -23,6 +23,7 @@
 #include <signal.h>
 #include <unistd.h>
 
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -138,6 +139,10 @@ int main(int argc, char** argv) {
         CK(cuMemAllocPitch(&flags, &flags_pitch, (size_t)G * sizeof(int), G, 16));
         CK(cuMemsetD2D8(flags, flags_pitch, 0, (size_t)G * sizeof(int), G));
     }
+    // timed like the reference's main times its call (main.cu:225-232):
+    // from the queue allocation to after the queue is freed
+    CK(cuCtxSynchronize());
+    const auto t_start = std::chrono::steady_clock::now();
     {
         void* args[] = {&gq};
         launch(k_alloc, 1, 1, 1, 1, args);
@@ -183,6 +188,7 @@ int main(int argc, char** argv) {
         launch(k_free, 1, 1, 1, 1, args);
         CK(cuCtxSynchronize());
     }
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
 
     std::vector<unsigned char> out((size_t)size * size);
     CUDA_MEMCPY2D back;
@@ -202,8 +208,8 @@ int main(int argc, char** argv) {
         return 4;
     }
     std::fclose(f);
-    std::printf("{\"variant\": \"%s\", \"size\": %d, \"rounds\": %lld, \"restarts\": %d}\n", variant.c_str(), size,
-                rounds, restarts);
+    std::printf("{\"variant\": \"%s\", \"size\": %d, \"rounds\": %lld, \"restarts\": %d, \"ms\": %.3f}\n",
+                variant.c_str(), size, rounds, restarts, ms);
     cuMemFree(d_marker);
     cuMemFree(d_mask);
     cuMemFree(gq);
