@@ -450,26 +450,33 @@ __device__ void async_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
                 const unsigned slot = (p - a.G) % a.cap;
                 long long idle_since = globaltimer_ns();
                 unsigned idle_progress = ld_volatile(&a.ctrl->progress);
-                unsigned ns = 32;
+                unsigned ns = 32, spins = 0;
                 for (;;) {
-                    v = atomicExch(&a.q0[slot], 0u);
-                    if (v != 0u) break;
-                    if (ld_volatile(&a.ctrl->pending) == 0 || ld_volatile(&a.ctrl->error) != 0u) {
-                        verdict = 1;
+                    // The slot is this warp's alone: watch it with plain loads
+                    // (a waiting warp issues no atomics) and take it once set.
+                    if (ld_volatile(&a.q0[slot]) != 0u) {
+                        v = atomicExch(&a.q0[slot], 0u);
                         break;
+                    }
+                    // the job's counters every eighth look
+                    if ((++spins & 7u) == 0u) {
+                        if (ld_volatile(&a.ctrl->pending) == 0 || ld_volatile(&a.ctrl->error) != 0u) {
+                            verdict = 1;
+                            break;
+                        }
+                        const unsigned prog = ld_volatile(&a.ctrl->progress);
+                        const long long now = globaltimer_ns();
+                        if (prog != idle_progress) {
+                            idle_progress = prog;
+                            idle_since = now;
+                        } else if (now - idle_since > a.timeout_ns) {
+                            set_error(a.ctrl, DEV_ERR_TIMEOUT);
+                            verdict = 1;
+                            break;
+                        }
                     }
                     __nanosleep(ns);
                     if (ns < 256) ns <<= 1;
-                    const unsigned prog = ld_volatile(&a.ctrl->progress);
-                    const long long now = globaltimer_ns();
-                    if (prog != idle_progress) {
-                        idle_progress = prog;
-                        idle_since = now;
-                    } else if (now - idle_since > a.timeout_ns) {
-                        set_error(a.ctrl, DEV_ERR_TIMEOUT);
-                        verdict = 1;
-                        break;
-                    }
                 }
             }
             verdict = __shfl_sync(FULL, verdict, 0);
