@@ -40,6 +40,7 @@ pixels / max time.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -344,14 +345,19 @@ def bench_served(args, dev, variant):
 
     # plain per-request calls, closed loop, same pinned host buffers
     torch.cuda.synchronize()
-    t = time.perf_counter()
-    for w in which:
-        m, k = pin[w]
-        dm, dk = _to_dev(m, dev), _to_dev(k, dev)
-        iwpp.reconstruct(dm, dk, connectivity=8, variant=variant, handle=h)
-        o = outs[w]
-        torch.from_numpy(o.view(np.int16) if o.dtype == np.uint16 else o).copy_(dm)
-    t_plain = time.perf_counter() - t
+    gc.collect()
+    gc.disable()
+    try:
+        t = time.perf_counter()
+        for w in which:
+            m, k = pin[w]
+            dm, dk = _to_dev(m, dev), _to_dev(k, dev)
+            iwpp.reconstruct(dm, dk, connectivity=8, variant=variant, handle=h)
+            o = outs[w]
+            torch.from_numpy(o.view(np.int16) if o.dtype == np.uint16 else o).copy_(dm)
+        t_plain = time.perf_counter() - t
+    finally:
+        gc.enable()
     plain_ok = all(np.array_equal(outs[w], refs[w]) for w in set(which))
     h.close()
 
@@ -361,19 +367,26 @@ def bench_served(args, dev, variant):
         with iwpp.Server(device=dev.index or 0, lanes=args.lanes, variant=variant) as srv:
             for w in range(len(specs)):  # warm the pool and the lanes
                 srv.wait(srv.submit(pin[w][0], pin[w][1], 8, out=outs[w]))
-            tickets = []
-            t0 = time.perf_counter()
-            for i, w in enumerate(which):
-                if open_loop:
-                    while time.perf_counter() - t0 < times[i]:
-                        pass
-                tickets.append(srv.submit(pin[w][0], pin[w][1], 8, out=outs[w]))
-            lat, status_ok = [], True
-            for tk in tickets:
-                _, info = srv.wait(tk)
-                lat.append(info["latency_us"] / 1e3)
-                status_ok &= info["status"] == 0
-            dt = time.perf_counter() - t0
+            # no collector pauses in the submitting loop: a pause would turn
+            # the Poisson stream into bursts
+            gc.collect()
+            gc.disable()
+            try:
+                tickets = []
+                t0 = time.perf_counter()
+                for i, w in enumerate(which):
+                    if open_loop:
+                        while time.perf_counter() - t0 < times[i]:
+                            pass
+                    tickets.append(srv.submit(pin[w][0], pin[w][1], 8, out=outs[w]))
+                lat, status_ok = [], True
+                for tk in tickets:
+                    _, info = srv.wait(tk)
+                    lat.append(info["latency_us"] / 1e3)
+                    status_ok &= info["status"] == 0
+                dt = time.perf_counter() - t0
+            finally:
+                gc.enable()
             st = srv.stats()
         ok = status_ok and all(np.array_equal(outs[w], refs[w]) for w in set(which))
         lat = np.array(lat)
