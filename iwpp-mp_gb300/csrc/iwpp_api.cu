@@ -367,6 +367,60 @@ int finish_staging(Job& job, cudaStream_t s) {
     return cuda_status(first);
 }
 
+// Pinned host slots for the descriptor uploads of asynchronous calls: a
+// copy from pageable memory makes the driver wait for the stream's earlier
+// work first, which would turn every asynchronous call into a synchronous
+// one.  Two slots alternate; a slot is reused once its last upload is done.
+struct HostStaging {
+    void* p[2] = {nullptr, nullptr};
+    size_t bytes[2] = {0, 0};
+    cudaEvent_t done[2] = {nullptr, nullptr};
+    bool pending[2] = {false, false};
+    int next = 0;
+
+    char* acquire(size_t need, int* slot) {
+        const int k = next;
+        next ^= 1;
+        if (pending[k]) {
+            cudaEventSynchronize(done[k]);
+            pending[k] = false;
+        }
+        if (!done[k] && cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            done[k] = nullptr;
+            return nullptr;
+        }
+        if (bytes[k] < need) {
+            if (p[k]) cudaFreeHost(p[k]);
+            p[k] = nullptr;
+            bytes[k] = 0;
+            const size_t want = std::max<size_t>(need, 64u << 10);
+            if (cudaMallocHost(&p[k], want) != cudaSuccess) {
+                cudaGetLastError();
+                p[k] = nullptr;
+                return nullptr;
+            }
+            bytes[k] = want;
+        }
+        *slot = k;
+        return static_cast<char*>(p[k]);
+    }
+    void mark(int k, cudaStream_t s) {
+        if (cudaEventRecord(done[k], s) == cudaSuccess) pending[k] = true;
+    }
+    void release() {
+        for (int k = 0; k < 2; ++k) {
+            if (pending[k]) cudaEventSynchronize(done[k]);
+            if (p[k]) cudaFreeHost(p[k]);
+            if (done[k]) cudaEventDestroy(done[k]);
+            p[k] = nullptr;
+            done[k] = nullptr;
+            bytes[k] = 0;
+            pending[k] = false;
+        }
+    }
+};
+
 }  // namespace
 
 struct iwpp_handle_s {
@@ -374,6 +428,7 @@ struct iwpp_handle_s {
     Workspace ws;
     Ctrl* host_ctrl = nullptr;  // pinned
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    HostStaging staging;
     cudaStream_t last_stream = nullptr;
     long long last_tiles = 0;
     int last_variant = IWPP_QUEUE_UNIQUE;
@@ -429,7 +484,7 @@ int check_device(int device) {
 
 // Enqueues a prepared job on `s` into workspace `ws`.
 int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool use_events, cudaEvent_t ev0,
-                cudaEvent_t ev1, bool upload_descs) {
+                cudaEvent_t ev1, bool upload_descs, HostStaging* hs = nullptr) {
     const bool two = job.variant == IWPP_QUEUE_DOUBLE || job.variant == IWPP_QUEUE_UNIQUE;
     const long long cap = job_queue_capacity(job);
     const Layout l = layout_for((long long)job.descs.size(), job.G, cap, two);
@@ -454,11 +509,20 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
         std::vector<ImgDesc> descs = job.descs;
         for (size_t i = 0; i < descs.size(); ++i)
             descs[i].tmaps = job.has_tma[i] ? base + l.off_tmaps + i * 2u * sizeof(CUtensorMap) : nullptr;
-        e = cudaMemcpyAsync(base + l.off_tmaps, job.tmaps.data(), job.tmaps.size() * sizeof(CUtensorMap),
-                            cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(base + l.off_imgs, descs.data(), descs.size() * sizeof(ImgDesc),
-                                cudaMemcpyHostToDevice, s);
+        const size_t tb = job.tmaps.size() * sizeof(CUtensorMap), db = descs.size() * sizeof(ImgDesc);
+        int slot = -1;
+        char* pin = hs ? hs->acquire(tb + db, &slot) : nullptr;
+        const void* src_t = job.tmaps.data();
+        const void* src_d = descs.data();
+        if (pin) {
+            std::memcpy(pin, job.tmaps.data(), tb);
+            std::memcpy(pin + tb, descs.data(), db);
+            src_t = pin;
+            src_d = pin + tb;
+        }
+        e = cudaMemcpyAsync(base + l.off_tmaps, src_t, tb, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(base + l.off_imgs, src_d, db, cudaMemcpyHostToDevice, s);
+        if (pin) hs->mark(slot, s);
     }
     if (e != cudaSuccess) return cuda_status(e);
     if (use_events) cudaEventRecord(ev0, s);
@@ -567,7 +631,7 @@ int run_job_sync(iwpp_handle h, const iwpp_image* imgs, int n, int variant, cons
     if (prev_dev != h->device) cudaSetDevice(h->device);
     Job job;
     rc = build_job(job, imgs, n, variant, cfg, s, STAGE_ASYNC);
-    if (rc == IWPP_OK) rc = enqueue_job(job, h->ws, s, h->device, true, h->ev0, h->ev1, true);
+    if (rc == IWPP_OK) rc = enqueue_job(job, h->ws, s, h->device, true, h->ev0, h->ev1, true, &h->staging);
     const int rc_stage = finish_staging(job, s);
     if (rc == IWPP_OK) {
         float ms = 0.f;
@@ -653,6 +717,7 @@ int iwpp_handle_destroy(iwpp_handle h) {
     cudaGetDevice(&prev);
     cudaSetDevice(h->device);
     cudaDeviceSynchronize();
+    h->staging.release();
     if (h->ws.base) cudaFree(h->ws.base);
     if (h->host_ctrl) cudaFreeHost(h->host_ctrl);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -697,7 +762,7 @@ int iwpp_reconstruct_batch_async(iwpp_handle h, const iwpp_image* images, int n,
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     Job job;
     int rc = build_job(job, images, n, variant, cfg, s, STAGE_ASYNC);
-    if (rc == IWPP_OK) rc = enqueue_job(job, h->ws, s, h->device, true, h->ev0, h->ev1, true);
+    if (rc == IWPP_OK) rc = enqueue_job(job, h->ws, s, h->device, true, h->ev0, h->ev1, true, &h->staging);
     const int rc2 = finish_staging(job, s);
     if (rc == IWPP_OK) rc = rc2;
     if (rc == IWPP_OK && h->ws.base) {
@@ -987,7 +1052,7 @@ int iwpp_autotune(iwpp_handle h, const iwpp_image* images, int n, int variant, i
             if (restore() != IWPP_OK) return -1.0;
             Job job;
             int jrc = build_job(job, images, n, v, &c, s, STAGE_ASYNC, false);
-            if (jrc == IWPP_OK) jrc = enqueue_job(job, h->ws, s, h->device, true, h->ev0, h->ev1, true);
+            if (jrc == IWPP_OK) jrc = enqueue_job(job, h->ws, s, h->device, true, h->ev0, h->ev1, true, &h->staging);
             const int src = finish_staging(job, s);
             if (jrc == IWPP_OK) jrc = src;
             if (jrc != IWPP_OK) {
@@ -1068,7 +1133,7 @@ int iwpp_autotune(iwpp_handle h, const iwpp_image* images, int n, int variant, i
         if (rc == IWPP_OK) {
             Job job;
             rc = build_job(job, images, n, v, &best, s, STAGE_ASYNC, false);
-            if (rc == IWPP_OK) rc = enqueue_job(job, h->ws, s, h->device, false, h->ev0, h->ev1, true);
+            if (rc == IWPP_OK) rc = enqueue_job(job, h->ws, s, h->device, false, h->ev0, h->ev1, true, &h->staging);
             const int src = finish_staging(job, s);
             if (rc == IWPP_OK) rc = src;
             if (cudaStreamSynchronize(s) != cudaSuccess && rc == IWPP_OK) rc = IWPP_ERR_CUDA;
