@@ -365,6 +365,7 @@ def bench_served(args, dev, variant):
     h.close()
 
     def run(open_loop):
+        clocks = ClockSampler(dev.index or 0)
         for o in outs:
             o.fill(0)
         with iwpp.Server(device=dev.index or 0, lanes=args.lanes, variant=variant) as srv:
@@ -374,6 +375,7 @@ def bench_served(args, dev, variant):
             # the Poisson stream into bursts
             gc.collect()
             gc.disable()
+            clocks.start()
             try:
                 tickets = []
                 t0 = time.perf_counter()
@@ -382,20 +384,27 @@ def bench_served(args, dev, variant):
                         while time.perf_counter() - t0 < times[i]:
                             pass
                     tickets.append(srv.submit(pin[w][0], pin[w][1], 8, out=outs[w]))
-                lat, status_ok = [], True
+                lat, queue, service, status_ok = [], [], [], True
                 for tk in tickets:
                     _, info = srv.wait(tk)
                     lat.append(info["latency_us"] / 1e3)
+                    queue.append(info["queue_us"] / 1e3)
+                    service.append(info["service_us"] / 1e3)
                     status_ok &= info["status"] == 0
                 dt = time.perf_counter() - t0
             finally:
                 gc.enable()
+                clock_info = clocks.stop()
             st = srv.stats()
         ok = status_ok and all(np.array_equal(outs[w], refs[w]) for w in set(which))
         lat = np.array(lat)
         return {"gpx_s": px / dt / 1e9, "seconds": dt, "p50_ms": float(np.percentile(lat, 50)),
-                "p99_ms": float(np.percentile(lat, 99)), "batches": st["batches"],
-                "largest_batch": st["largest_batch"], "device_bytes_peak": st["bytes_peak"], "bitexact": ok}
+                "p99_ms": float(np.percentile(lat, 99)),
+                "queue_p50_ms": float(np.percentile(queue, 50)), "queue_p99_ms": float(np.percentile(queue, 99)),
+                "service_p50_ms": float(np.percentile(service, 50)),
+                "service_p99_ms": float(np.percentile(service, 99)), "batches": st["batches"],
+                "largest_batch": st["largest_batch"], "device_bytes_peak": st["bytes_peak"], "bitexact": ok,
+                "clocks": clock_info}
 
     served = run(True)
     saturated = run(False)

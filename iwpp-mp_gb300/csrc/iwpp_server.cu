@@ -264,6 +264,19 @@ int iwpp_server_create(iwpp_server* out, int device, const iwpp_server_config* c
             rc = IWPP_ERR_CUDA;
         if (rc == IWPP_OK && ws_bytes > 0) rc = iwpp::handle_reserve(L.handle, (size_t)ws_bytes);
     }
+    if (rc == IWPP_OK && !s->lanes.empty()) {
+        // Map part of the budget into the pool now, so that admitting more
+        // requests at once than ever before does not stall a lane on the
+        // driver growing the pool in the middle of serving.
+        const size_t warm = (size_t)std::min<long long>(s->budget, 4ll << 30);
+        cudaStream_t ws = s->lanes[0].stream;
+        void* p = nullptr;
+        if (warm > 0 && cudaMallocFromPoolAsync(&p, warm, s->pool, ws) == cudaSuccess) {
+            cudaFreeAsync(p, ws);
+            cudaStreamSynchronize(ws);
+        }
+        cudaGetLastError();  // a pool that cannot be warmed still serves
+    }
     cudaSetDevice(prev);
     if (probe) iwpp_handle_destroy(probe);
     if (rc != IWPP_OK) {
