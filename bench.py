@@ -406,7 +406,12 @@ def bench_served(args, dev, variant):
                 "largest_batch": st["largest_batch"], "device_bytes_peak": st["bytes_peak"], "bitexact": ok,
                 "clocks": clock_info}
 
-    served = run(True)
+    # the open loop three times, the run with the median p99 reported: the
+    # host-to-device path of a shared box has slow moments of its own
+    opens = sorted((run(True) for _ in range(3)), key=lambda r: r["p99_ms"])
+    served = dict(opens[1])
+    served["p99_ms_of_runs"] = [r["p99_ms"] for r in opens]
+    served["bitexact"] = all(r["bitexact"] for r in opens)
     saturated = run(False)
     return {"workload": f"{n_req} requests, Poisson 2000/s (seed 4), sides log-uniform 256..8192 "
                         f"({px / n_req / 1e6:.2f} Mpx mean), uint8 80% / uint16 20%, 8-conn, "
@@ -655,7 +660,7 @@ def run_ours(args):
     }
     handle.close()
     if not args.no_extras:
-        for key, fn in (("batched", bench_batched), ("served", bench_served), ("spiral", bench_spiral)):
+        for key, fn in (("served", bench_served), ("batched", bench_batched), ("spiral", bench_spiral)):
             try:
                 line[key] = fn(args, dev, variant)
             except Exception as exc:  # reported in the line, the headline stands
