@@ -523,6 +523,7 @@ struct VisitResult {
     unsigned sweeps;     // sweeps run
     unsigned row_steps;  // rows processed by the sweeps
     bool ok;             // false: a bounded wait ran out (job error)
+    bool stored;         // rows of the tile were stored at the end of the visit
     long long t_fetch, t_proc, t_dump;  // clock64 cycles per phase
 };
 
@@ -672,7 +673,7 @@ __device__ __noinline__ VisitResult visit_tile(const ImgDesc& d, int tx, int ty,
                                                unsigned& phase, long long timeout_ns, unsigned sides, Early& early) {
     using P = Px<DT>;
     constexpr int TW = 32 * P::PPW;
-    VisitResult res{0u, 0u, 0u, true, 0, 0, 0};
+    VisitResult res{0u, 0u, 0u, true, false, 0, 0, 0};
     const long long c0 = clock64();
     const int x0 = tx * TW, y0 = ty * TH;
     const int W = d.W, H = d.H;
@@ -875,6 +876,7 @@ __device__ __noinline__ VisitResult visit_tile(const ImgDesc& d, int tx, int ty,
 
     // ---- write back the rows that rose, then neighbour detection
     write_back_rows<DT, TH>(d, sm, lane, y0, rows, npx, col_off, pend_rows);
+    res.stored = true;
     const unsigned nb = detect_neighbours<DT, CONN, TH>(sm, lane, (pend_rows & TOP) != 0ull,
                                                         (pend_rows & BOT) != 0ull, __any_sync(FULL, col_changed));
     __syncwarp();

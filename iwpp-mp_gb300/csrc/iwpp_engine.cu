@@ -283,9 +283,13 @@ __device__ bool process_entry(const EngineArgs& a, unsigned g, WarpSmem<TH>& sm,
         cnt.phase[2] += r.t_proc;
         cnt.phase[3] += r.t_dump;
         const long long q0 = clock64();
-        if (r.nb != 0u) {
-            __threadfence();  // release: this tile's stores before the neighbours' DIRTY
+        if (r.nb != 0u || r.stored) {
+            // release: this tile's stores before the neighbours' DIRTY and
+            // before the tile's ACTIVE bit clears (its next owner reads them)
+            __threadfence();
             __syncwarp();
+        }
+        if (r.nb != 0u) {
             const unsigned cont = notify<VAR>(a, d, tx, ty, r.nb, lane, wq, cnt);
             if (next) *next = cont;
         }
