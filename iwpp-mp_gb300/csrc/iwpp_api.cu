@@ -534,9 +534,14 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
     for (int p = 0; p < job.cfg.init_passes; ++p)
         for (const auto& d : job.descs)
             for (int dir = 0; dir < 4; ++dir) {
-                // raster (+X, +Y) then anti-raster (-X, -Y)
+                // raster (+X, +Y) then anti-raster (-X, -Y).  The vertical
+                // sweeps take the pixel above / below only: a valid update
+                // for either connectivity with no shuffle on the column
+                // chain; the tile engine completes the diagonals.
                 static const int order[4] = {0, 1, 2, 3};
-                e = launch_sweep(d, order[dir], s);
+                ImgDesc dv = d;
+                dv.conn = 4;
+                e = launch_sweep(dv, order[dir], s);
                 if (e != cudaSuccess) return cuda_status(e);
             }
     e = engine_launch_init(a, job.variant, s);

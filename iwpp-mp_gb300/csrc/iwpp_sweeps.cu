@@ -8,7 +8,8 @@
 //         rule m = max(m, min(prev, mask)) along one axis.
 //   +X / -X: one warp per row, the whole row as one max-min scan (128-byte
 //            chunks, carry from chunk to chunk), exact and coalesced.
-//   +Y / -Y: one warp per 128-byte column strip walking the full height;
+//   +Y / -Y: one warp per 128-byte column strip walking the full height,
+//            rows streamed through shared memory with cp.async far ahead;
 //            8-connectivity also takes the two diagonal pixels of the
 //            previous row inside the strip.  Every pixel is written by one
 //            thread, so the result is deterministic.
@@ -124,47 +125,252 @@ __global__ void sweep_x_kernel(ImgDesc d) {
 }
 
 // --------------------------------------------------------------- Y sweeps
+// 4-byte asynchronous global -> shared copy (cp.async, LDGSTS) and its
+// group bookkeeping.
+__device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(smem_dst)), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem_dst)), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// One warp per 128-byte column strip, walking the full height.  The chain
+// through the rows is a few operations per row; memory latency is hidden by
+// a ring of kRing rows per plane in shared memory, filled with cp.async
+// kRing rows ahead (groups of kGroup rows).  Each lane reads and writes its
+// own word of every row only, so no row is read after this thread wrote it.
+constexpr int kRing = 64, kGroup = 8;
+
 template <int DT, int CONN, bool DOWN>
-__global__ void sweep_y_kernel(ImgDesc d) {
+__global__ void __launch_bounds__(32) sweep_y_kernel(ImgDesc d) {
     using P = Px<DT>;
     constexpr int TW = 32 * P::PPW;
     constexpr int N = P::PPW;
+    constexpr int NG = kRing / kGroup;
+    __shared__ uint32_t ring_m[kRing][32];
+    __shared__ uint32_t ring_k[kRing][32];
     const int lane = threadIdx.x & 31;
-    const int strip = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int strip = (int)blockIdx.x;
     const int strips = (d.W + TW - 1) / TW;
     if (strip >= strips) return;
     const int px0 = strip * TW + lane * P::PPW, npx = d.W - px0;
     const size_t off = (size_t)(npx > 0 ? px0 : 0) * P::BPP;
+    const int H = d.H;
+    auto row_of = [&](int i) { return DOWN ? i : H - 1 - i; };
+    // row i (in sweep order) into slot i % kRing: a full word asynchronously,
+    // a partial word (right edge) or a word past the image by plain loads
+    auto issue = [&](int i) {
+        const int slot = i % kRing;
+        if (i >= H) return;
+        const int y = row_of(i);
+        const unsigned char* mrow = d.marker + (size_t)y * d.pitch_m + off;
+        const unsigned char* krow = d.mask + (size_t)y * d.pitch_k + off;
+        if (npx >= P::PPW) {
+            cp_async4(&ring_m[slot][lane], mrow);
+            cp_async4(&ring_k[slot][lane], krow);
+        } else {
+            uint32_t mw = P::MINW, kw = P::MINW;
+            if (npx > 0) load_pair<DT>(mrow, krow, npx, mw, kw);
+            ring_m[slot][lane] = mw;
+            ring_k[slot][lane] = kw;
+        }
+    };
+    for (int g = 0; g < NG; ++g) {
+        for (int q = 0; q < kGroup; ++q) issue(g * kGroup + q);
+        cp_async_commit();
+    }
     uint32_t prev[N];
 #pragma unroll
     for (int j = 0; j < N; ++j) prev[j] = P::MINPX;
-    for (int i = 0; i < d.H; ++i) {
-        const int y = DOWN ? i : d.H - 1 - i;
-        uint32_t mw = P::MINW, kw = P::MINW;
-        unsigned char* mrow = d.marker + (size_t)y * d.pitch_m + off;
-        if (npx > 0) load_pair<DT>(mrow, d.mask + (size_t)y * d.pitch_k + off, npx, mw, kw);
-        uint32_t m[N], k[N];
-        P::unpack(mw, m);
-        P::unpack(kw, k);
-        if (CONN == 8) {
-            uint32_t left = __shfl_up_sync(FULL, prev[N - 1], 1), right = __shfl_down_sync(FULL, prev[0], 1);
-            if (lane == 0) left = P::MINPX;
-            if (lane == 31) right = P::MINPX;
+    for (int base = 0; base < H; base += kGroup) {
+        cp_async_wait<NG - 1>();  // the group holding rows base .. base + kGroup - 1
+        __syncwarp();
+        // Straight-line code for the group: all ring reads first, then the
+        // chain through the rows (two operations per pixel), then the
+        // stores; rows past the image are computed on stale slots and not
+        // stored.
+        const int sb = base % kRing;
+        uint32_t mw[kGroup], kw[kGroup], out[kGroup];
 #pragma unroll
-            for (int j = 0; j < N; ++j) {
-                const uint32_t a = j == 0 ? left : prev[j - 1];
-                const uint32_t b = j == N - 1 ? right : prev[j + 1];
-                m[j] = P::mx(m[j], P::mn(P::mx3(a, prev[j], b), k[j]));
+        for (int q = 0; q < kGroup; ++q) {
+            mw[q] = ring_m[sb + q][lane];
+            kw[q] = ring_k[sb + q][lane];
+        }
+#pragma unroll
+        for (int q = 0; q < kGroup; ++q) {
+            uint32_t m[N], k[N];
+            P::unpack(mw[q], m);
+            P::unpack(kw[q], k);
+            if (CONN == 8) {
+                uint32_t left = __shfl_up_sync(FULL, prev[N - 1], 1), right = __shfl_down_sync(FULL, prev[0], 1);
+                if (lane == 0) left = P::MINPX;
+                if (lane == 31) right = P::MINPX;
+#pragma unroll
+                for (int j = 0; j < N; ++j) {
+                    const uint32_t a = j == 0 ? left : prev[j - 1];
+                    const uint32_t b = j == N - 1 ? right : prev[j + 1];
+                    m[j] = P::mx(m[j], P::mn(P::mx3(a, prev[j], b), k[j]));
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < N; ++j) m[j] = P::mx(m[j], P::mn(prev[j], k[j]));
+            }
+            out[q] = P::pack(m);
+#pragma unroll
+            for (int j = 0; j < N; ++j) prev[j] = m[j];
+        }
+#pragma unroll
+        for (int q = 0; q < kGroup; ++q)
+            if (base + q < H && npx > 0 && out[q] != mw[q])
+                store_word_plain<DT>(d.marker + (size_t)row_of(base + q) * d.pitch_m + off, npx, out[q]);
+        __syncwarp();  // the slots just read are refilled next
+        for (int q = 0; q < kGroup; ++q) issue(base + kRing + q);
+        cp_async_commit();
+    }
+    cp_async_wait<0>();
+}
+
+// Vertical sweep for 4-connectivity (the whole-image init passes use it for
+// either connectivity: the pixel above / below alone is a valid update).
+// Same streaming as sweep_y_kernel, but the chain through the rows is two
+// SIMD operations per register: uint8 words are held as two u16x2 halves
+// (min / max on 16-bit pairs are single instructions), uint16 words are
+// u16x2 already, int32 is one signed pixel.  Stores are unconditional.
+template <int DT>
+struct Lanes4;
+template <>
+struct Lanes4<DT_U8> {
+    static constexpr int R = 2;  // registers per word
+    __device__ static __forceinline__ void split(uint32_t w, uint32_t (&r)[2]) {
+        r[0] = __byte_perm(w, 0u, 0x4140);  // pixels 0, 1 as u16x2
+        r[1] = __byte_perm(w, 0u, 0x4342);  // pixels 2, 3
+    }
+    __device__ static __forceinline__ uint32_t join(const uint32_t (&r)[2]) { return __byte_perm(r[0], r[1], 0x6420); }
+    __device__ static __forceinline__ uint32_t mn(uint32_t a, uint32_t b) { return __vminu2(a, b); }
+    __device__ static __forceinline__ uint32_t mx(uint32_t a, uint32_t b) { return __vmaxu2(a, b); }
+    static constexpr uint32_t MIN = 0u;
+};
+template <>
+struct Lanes4<DT_U16> {
+    static constexpr int R = 1;
+    __device__ static __forceinline__ void split(uint32_t w, uint32_t (&r)[1]) { r[0] = w; }
+    __device__ static __forceinline__ uint32_t join(const uint32_t (&r)[1]) { return r[0]; }
+    __device__ static __forceinline__ uint32_t mn(uint32_t a, uint32_t b) { return __vminu2(a, b); }
+    __device__ static __forceinline__ uint32_t mx(uint32_t a, uint32_t b) { return __vmaxu2(a, b); }
+    static constexpr uint32_t MIN = 0u;
+};
+template <>
+struct Lanes4<DT_I32> {
+    static constexpr int R = 1;
+    __device__ static __forceinline__ void split(uint32_t w, uint32_t (&r)[1]) { r[0] = w; }
+    __device__ static __forceinline__ uint32_t join(const uint32_t (&r)[1]) { return r[0]; }
+    __device__ static __forceinline__ uint32_t mn(uint32_t a, uint32_t b) { return (uint32_t)min((int)a, (int)b); }
+    __device__ static __forceinline__ uint32_t mx(uint32_t a, uint32_t b) { return (uint32_t)max((int)a, (int)b); }
+    static constexpr uint32_t MIN = 0x80000000u;
+};
+
+template <int DT, bool DOWN>
+__global__ void __launch_bounds__(32) sweep_y4_kernel(ImgDesc d) {
+    using P = Px<DT>;
+    using L = Lanes4<DT>;
+    constexpr int TW = 32 * P::PPW;
+    constexpr int R = L::R;
+    constexpr int NG = kRing / kGroup;
+    __shared__ __align__(16) uint32_t ring_m[kRing][32];
+    __shared__ __align__(16) uint32_t ring_k[kRing][32];
+    const int lane = threadIdx.x & 31;
+    const int strip = (int)blockIdx.x;
+    const int px0 = strip * TW + lane * P::PPW, npx = d.W - px0;
+    const size_t off = (size_t)(npx > 0 ? px0 : 0) * P::BPP;
+    const int H = d.H;
+    const long long step_m = DOWN ? d.pitch_m : -d.pitch_m, step_k = DOWN ? d.pitch_k : -d.pitch_k;
+    const unsigned char* m0 = d.marker + (size_t)(DOWN ? 0 : H - 1) * d.pitch_m + off;
+    const unsigned char* k0 = d.mask + (size_t)(DOWN ? 0 : H - 1) * d.pitch_k + off;
+    // Whole 128-byte rows of the strip in 16-byte pieces (lane = piece of a
+    // row: 8 pieces per row and plane, 4 rows per instruction) when the
+    // strip lies inside every row and both planes are 16-byte aligned;
+    // otherwise one 4-byte word per lane and row.
+    const unsigned char* sm0 = d.marker + (size_t)(DOWN ? 0 : H - 1) * d.pitch_m + (size_t)strip * 128u;
+    const unsigned char* sk0 = d.mask + (size_t)(DOWN ? 0 : H - 1) * d.pitch_k + (size_t)strip * 128u;
+    const bool wide = (long long)(strip + 1) * 128 <= (long long)d.W * P::BPP &&
+                      ((reinterpret_cast<uintptr_t>(d.marker) | reinterpret_cast<uintptr_t>(d.mask)) & 15u) == 0u &&
+                      ((d.pitch_m | d.pitch_k) & 15) == 0;
+    auto issue_group = [&](int g0) {  // rows g0 .. g0 + kGroup - 1 (those below H)
+        if (wide) {
+            const int piece = lane & 7;
+#pragma unroll
+            for (int rr = 0; rr < kGroup; rr += 4) {
+                const int i = g0 + rr + (lane >> 3);
+                if (i < H) {
+                    const int slot = i % kRing;
+                    cp_async16(&ring_m[slot][piece * 4], sm0 + (long long)i * step_m + piece * 16);
+                    cp_async16(&ring_k[slot][piece * 4], sk0 + (long long)i * step_k + piece * 16);
+                }
             }
         } else {
-#pragma unroll
-            for (int j = 0; j < N; ++j) m[j] = P::mx(m[j], P::mn(prev[j], k[j]));
+            for (int q = 0; q < kGroup; ++q) {
+                const int i = g0 + q;
+                if (i >= H) break;
+                const int slot = i % kRing;
+                const unsigned char* mrow = m0 + (long long)i * step_m;
+                const unsigned char* krow = k0 + (long long)i * step_k;
+                if (npx >= P::PPW) {
+                    cp_async4(&ring_m[slot][lane], mrow);
+                    cp_async4(&ring_k[slot][lane], krow);
+                } else {
+                    uint32_t mw = P::MINW, kw = P::MINW;
+                    if (npx > 0) load_pair<DT>(mrow, krow, npx, mw, kw);
+                    ring_m[slot][lane] = mw;
+                    ring_k[slot][lane] = kw;
+                }
+            }
         }
-        const uint32_t x = P::pack(m);
-        if (npx > 0 && x != mw) store_word_plain<DT>(mrow, npx, x);
-#pragma unroll
-        for (int j = 0; j < N; ++j) prev[j] = m[j];
+    };
+    for (int g = 0; g < NG; ++g) {
+        issue_group(g * kGroup);
+        cp_async_commit();
     }
+    uint32_t prev[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) prev[j] = L::MIN;
+    for (int base = 0; base < H; base += kGroup) {
+        cp_async_wait<NG - 1>();
+        __syncwarp();  // pieces copied by other lanes are visible to this one
+        const int sb = base % kRing;
+        uint32_t out[kGroup];
+#pragma unroll
+        for (int q = 0; q < kGroup; ++q) {
+            uint32_t m[R], k[R];
+            L::split(ring_m[sb + q][lane], m);
+            L::split(ring_k[sb + q][lane], k);
+#pragma unroll
+            for (int j = 0; j < R; ++j) {
+                m[j] = L::mx(m[j], L::mn(prev[j], k[j]));
+                prev[j] = m[j];
+            }
+            out[q] = L::join(m);
+        }
+        if (npx >= P::PPW) {
+#pragma unroll
+            for (int q = 0; q < kGroup; ++q)
+                if (base + q < H)
+                    *reinterpret_cast<uint32_t*>(const_cast<unsigned char*>(m0) + (long long)(base + q) * step_m) =
+                        out[q];
+        } else if (npx > 0) {
+            for (int q = 0; q < kGroup; ++q)
+                if (base + q < H)
+                    store_word_plain<DT>(const_cast<unsigned char*>(m0) + (long long)(base + q) * step_m, npx, out[q]);
+        }
+        __syncwarp();  // the slots just read are refilled next
+        issue_group(base + kRing);
+        cp_async_commit();
+    }
+    cp_async_wait<0>();
 }
 
 // ------------------------------------------------------------ host side
@@ -215,18 +421,18 @@ static void launch_sweep_t(const ImgDesc& d, int direction, cudaStream_t s) {
             sweep_x_kernel<DT, false><<<blocks, 128, 0, s>>>(d);
     } else {
         const int strips = (d.W + TW - 1) / TW;
-        const unsigned blocks = blocks_for((long long)strips * 32, 64);
+        const unsigned blocks = (unsigned)strips;
         const bool down = direction == 1;
         if (d.conn == 8) {
             if (down)
-                sweep_y_kernel<DT, 8, true><<<blocks, 64, 0, s>>>(d);
+                sweep_y_kernel<DT, 8, true><<<blocks, 32, 0, s>>>(d);
             else
-                sweep_y_kernel<DT, 8, false><<<blocks, 64, 0, s>>>(d);
+                sweep_y_kernel<DT, 8, false><<<blocks, 32, 0, s>>>(d);
         } else {
             if (down)
-                sweep_y_kernel<DT, 4, true><<<blocks, 64, 0, s>>>(d);
+                sweep_y4_kernel<DT, true><<<blocks, 32, 0, s>>>(d);
             else
-                sweep_y_kernel<DT, 4, false><<<blocks, 64, 0, s>>>(d);
+                sweep_y4_kernel<DT, false><<<blocks, 32, 0, s>>>(d);
         }
     }
 }
