@@ -455,6 +455,11 @@ def bench_spiral(args, dev, variant):
         bpp = mask.dtype.itemsize
         m0, k = _to_dev(marker, dev), _to_dev(mask, dev)
         m = m0.clone()
+        # the untuned default first, then the autotuned configuration for
+        # this image class (tile rows, solver, initial whole-image passes)
+        st0 = iwpp.reconstruct(m, k, connectivity=8, variant=variant, handle=h)
+        m.copy_(m0)
+        tuned = iwpp.autotune([(m, k, 8)], variant=variant, repeats=1, handle=h)
         times = []
         for rep in range(1 + args.spiral_reps):
             m.copy_(m0)
@@ -464,7 +469,8 @@ def bench_spiral(args, dev, variant):
                 times.append(st.device_ms)
         t = statistics.median(times) / 1e3
         entry = {"ms": t * 1e3, "gpx_s": W * H / t / 1e9, "hbm_frac": 3 * W * H * bpp / t / 1e9 / peak,
-                 "visits": st.visits, "tiles": st.tiles}
+                 "visits": st.visits, "tiles": st.tiles, "untuned_ms": st0.device_ms,
+                 "autotuned": {k_: tuned[k_] for k_ in ("tile_rows", "solver", "init_passes")}}
         if name == "u8" and not args.no_cpu:
             import oracle
 
@@ -479,7 +485,8 @@ def bench_spiral(args, dev, variant):
     h.close()
     res["workload"] = ("16384x16384, 8-conn, smoothed noise (seed 2, sigma 16) with a 1-px spiral corridor "
                        "(arm pitch 256) at the dtype maximum, marker 0 but 64 seeds; device time per "
-                       f"reconstruction, median of {args.spiral_reps}")
+                       f"reconstruction with the autotuned configuration, median of {args.spiral_reps} "
+                       "(untuned_ms: the default configuration)")
     return res
 
 

@@ -59,7 +59,7 @@ typedef struct iwpp_config {
     int tile_rows;             /* 32 or 64 rows per tile; 0 = default (64) */
     long long queue_capacity;  /* entries per queue buffer; 0 = default; < 0: that multiple
                                   of the job's tile count */
-    int init_passes;           /* whole-image raster + anti-raster pairs first; -1 = default */
+    int init_passes;           /* whole-image passes first (+X, +Y, -X, -Y each); -1 = default (0) */
     int grid_ctas;             /* persistent grid size; 0 = one full wave */
     int max_restarts;          /* queue-overflow restarts allowed; 0 = default (64) */
     int timeout_ms;            /* bound on every device-side wait; 0 = default (10000) */
@@ -168,8 +168,9 @@ IWPP_API int iwpp_queue_selftest(int device, int variant, int grid_side, int cop
  * initial passes are compile-time constants, IWPP MP/include/
  * MorphologicalReconstruction.cuh:6-7, and commented-out sweeps, MR.cu:792-795).
  * Times candidate configurations on the caller's own batch -- tile rows
- * 64 / 32 x in-tile solver, then 1 / 2 initial raster + anti-raster pass
- * pairs, then (mutex / double queues) queue capacity 1x / 16x the tiles --
+ * 64 / 32 x in-tile solver, then 1, 2, 4, ... 64 initial raster +
+ * anti-raster passes while each doubling is faster, then (mutex / double
+ * queues) queue capacity 1x / 16x the tiles --
  * each the median of `repeats` runs (0 = 3) from the same markers, records
  * the fastest in the process-wide tuning table under the batch's workload
  * class (queue variant, pixel type, connectivity, floor(log2(pixels)),

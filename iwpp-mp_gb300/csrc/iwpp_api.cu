@@ -1098,13 +1098,17 @@ int iwpp_autotune(iwpp_handle h, const iwpp_image* images, int n, int variant, i
                 c.init_passes = 0;
                 consider(c, th == 64 && solver == 0);
             }
-        // stage 2: initial whole-image raster / anti-raster pass pairs
+        // stage 2: initial whole-image raster / anti-raster passes, doubling
+        // while they pay (long corridors want one pass per turn of the
+        // front), stopping at the first count that does not beat the best
         if (best_ms >= 0.0) {
             const iwpp_config base = best;
-            for (int ip : {1, 2}) {
+            for (int ip = 1; ip <= 64; ip *= 2) {
                 iwpp_config c = base;
                 c.init_passes = ip;
+                const double before = best_ms;
                 consider(c, false);
+                if (!(best_ms < before)) break;
             }
         }
         // stage 3: queue capacity, for the queues whose capacity is free

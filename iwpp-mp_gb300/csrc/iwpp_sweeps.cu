@@ -373,6 +373,103 @@ __global__ void __launch_bounds__(32) sweep_y4_kernel(ImgDesc d) {
     cp_async_wait<0>();
 }
 
+constexpr int kRingN = 64;  // rows in flight per plane in the narrow variant
+
+// Narrow variant for uint8 / uint16: a warp covers a 64-byte strip, two
+// bytes per lane (uint8: two pixels as one u16x2 register; uint16: one
+// pixel), so the chain per row is one min and one max, and twice as many
+// warps share the image.
+template <int DT, bool DOWN>
+__global__ void __launch_bounds__(32) sweep_y4n_kernel(ImgDesc d) {
+    static_assert(DT == DT_U8 || DT == DT_U16, "two-byte lanes");
+    using P = Px<DT>;
+    constexpr int NR = kRingN, NG = kRingN / kGroup;
+    __shared__ __align__(16) uint16_t ring_m[kRingN][32];
+    __shared__ __align__(16) uint16_t ring_k[kRingN][32];
+    const int lane = threadIdx.x & 31;
+    const int strip = (int)blockIdx.x;
+    const long long row_bytes = (long long)d.W * P::BPP;
+    const long long b0 = (long long)strip * 64 + lane * 2;  // this lane's first byte in a row
+    const long long nbytes = row_bytes - b0;                 // >= 2: whole element, 1: half, <= 0: none
+    const int H = d.H;
+    const long long step_m = DOWN ? d.pitch_m : -d.pitch_m, step_k = DOWN ? d.pitch_k : -d.pitch_k;
+    const unsigned char* m0 = d.marker + (size_t)(DOWN ? 0 : H - 1) * d.pitch_m;
+    const unsigned char* k0 = d.mask + (size_t)(DOWN ? 0 : H - 1) * d.pitch_k;
+    const bool wide = (long long)(strip + 1) * 64 <= row_bytes &&
+                      ((reinterpret_cast<uintptr_t>(d.marker) | reinterpret_cast<uintptr_t>(d.mask)) & 15u) == 0u &&
+                      ((d.pitch_m | d.pitch_k) & 15) == 0;
+    auto issue_group = [&](int g0) {
+        if (wide) {  // 4 pieces of 16 bytes per row and plane, 8 rows per instruction
+            const int piece = lane & 3;
+            const int rr = lane >> 2;
+            const int i = g0 + rr;
+            if (i < H) {
+                const int slot = i % NR;
+                const long long o = (long long)strip * 64 + piece * 16;
+                cp_async16(&ring_m[slot][piece * 8], m0 + (long long)i * step_m + o);
+                cp_async16(&ring_k[slot][piece * 8], k0 + (long long)i * step_k + o);
+            }
+        } else {
+            for (int q = 0; q < kGroup; ++q) {
+                const int i = g0 + q;
+                if (i >= H) break;
+                const int slot = i % NR;
+                const unsigned char* mrow = m0 + (long long)i * step_m + (nbytes > 0 ? b0 : 0);
+                const unsigned char* krow = k0 + (long long)i * step_k + (nbytes > 0 ? b0 : 0);
+                uint16_t mv = 0, kv = 0;
+                if (nbytes >= 2) {
+                    mv = *reinterpret_cast<const uint16_t*>(mrow);
+                    kv = *reinterpret_cast<const uint16_t*>(krow);
+                } else if (nbytes == 1) {  // uint8 only: the last pixel of the row
+                    mv = *mrow;
+                    kv = *krow;
+                }
+                ring_m[slot][lane] = mv;
+                ring_k[slot][lane] = kv;
+            }
+        }
+    };
+    for (int g = 0; g < NG; ++g) {
+        issue_group(g * kGroup);
+        cp_async_commit();
+    }
+    uint32_t prev = 0u;
+    unsigned char* mo = const_cast<unsigned char*>(m0) + (nbytes > 0 ? b0 : 0);
+    for (int base = 0; base < H; base += kGroup) {
+        cp_async_wait<NG - 1>();
+        __syncwarp();
+        const int sb = base % NR;
+        uint32_t out[kGroup];
+#pragma unroll
+        for (int q = 0; q < kGroup; ++q) {
+            uint32_t m = ring_m[sb + q][lane], k = ring_k[sb + q][lane];
+            if (DT == DT_U8) {
+                m = __byte_perm(m, 0u, 0x4140);
+                k = __byte_perm(k, 0u, 0x4140);
+                m = __vmaxu2(m, __vminu2(prev, k));
+                prev = m;
+                out[q] = __byte_perm(m, 0u, 0x0020);
+            } else {
+                m = max(m, min(prev, k));
+                prev = m;
+                out[q] = m;
+            }
+        }
+        if (nbytes >= 2) {
+#pragma unroll
+            for (int q = 0; q < kGroup; ++q)
+                if (base + q < H) *reinterpret_cast<uint16_t*>(mo + (long long)(base + q) * step_m) = (uint16_t)out[q];
+        } else if (nbytes == 1) {
+            for (int q = 0; q < kGroup; ++q)
+                if (base + q < H) *(mo + (long long)(base + q) * step_m) = (unsigned char)out[q];
+        }
+        __syncwarp();
+        issue_group(base + NR);
+        cp_async_commit();
+    }
+    cp_async_wait<0>();
+}
+
 // ------------------------------------------------------------ host side
 static unsigned blocks_for(long long threads, int block) {
     long long b = (threads + block - 1) / block;
@@ -428,11 +525,18 @@ static void launch_sweep_t(const ImgDesc& d, int direction, cudaStream_t s) {
                 sweep_y_kernel<DT, 8, true><<<blocks, 32, 0, s>>>(d);
             else
                 sweep_y_kernel<DT, 8, false><<<blocks, 32, 0, s>>>(d);
-        } else {
+        } else if (DT == DT_I32) {
             if (down)
                 sweep_y4_kernel<DT, true><<<blocks, 32, 0, s>>>(d);
             else
                 sweep_y4_kernel<DT, false><<<blocks, 32, 0, s>>>(d);
+        } else {
+            constexpr int NDT = DT == DT_I32 ? DT_U8 : DT;  // (never i32 here)
+            const unsigned nblocks = (unsigned)(((long long)d.W * P::BPP + 63) / 64);
+            if (down)
+                sweep_y4n_kernel<NDT, true><<<nblocks, 32, 0, s>>>(d);
+            else
+                sweep_y4n_kernel<NDT, false><<<nblocks, 32, 0, s>>>(d);
         }
     }
 }

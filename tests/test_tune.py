@@ -116,7 +116,7 @@ def test_autotune_single_image(variant):
     m, k = _dev(marker), _dev(mask)
     res = iwpp.autotune([(m, k, 8)], variant=variant, repeats=1)
     assert np.array_equal(_host(m, marker.dtype), ref)
-    assert res["tile_rows"] in (32, 64) and res["solver"] in (0, 1, 2) and res["init_passes"] in (0, 1, 2)
+    assert res["tile_rows"] in (32, 64) and res["solver"] in (0, 1, 2) and 0 <= res["init_passes"] <= 64
     assert res["candidates"] >= 6 and res["best_ms"] > 0 and res["default_ms"] >= res["best_ms"]
     assert iwpp.tune_entries() == 1
     got = iwpp.tune_lookup(variant, 1, 8, 1500 * 1100)
