@@ -52,13 +52,17 @@ def test_fixed_point_checker(dt, conn):
     assert iwpp.fixed_point_violations(_dev(bad), k, conn) == 1
 
 
+@pytest.mark.parametrize("tuned", [False, True])
 @pytest.mark.parametrize("dt", [synth.U8, synth.U16, synth.I32])
-def test_spiral_16384_properties(dt):
+def test_spiral_16384_properties(dt, tuned):
     import torch
     marker, mask, n_corridor = synth.config2(dt)
     m0, k = _dev(marker), _dev(mask)
     m = m0.clone()
-    st = iwpp.reconstruct(m, k, connectivity=8)
+    # tuned: the configuration the autotuner picks for this image (32
+    # whole-image passes first, then the pass solver)
+    cfg = iwpp.Config.make(init_passes=32, solver=2) if tuned else None
+    st = iwpp.reconstruct(m, k, connectivity=8, config=cfg)
     assert st.status == 0
     assert iwpp.fixed_point_violations(m, k, 8) == 0
     if dt == synth.U16:
