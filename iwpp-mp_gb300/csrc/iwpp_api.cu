@@ -159,17 +159,19 @@ struct Workspace {
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 struct Layout {
-    size_t off_imgs, off_tmaps, off_state, off_q0, off_q1, total;
+    size_t off_imgs, off_tmaps, off_state, off_q0, off_q1, off_sweep, total;
 };
 
-Layout layout_for(long long n_imgs, long long G, long long cap, bool two_queues) {
+// sweep_bytes: scratch of the whole-image sweeps run before the engine
+Layout layout_for(long long n_imgs, long long G, long long cap, bool two_queues, size_t sweep_bytes = 0) {
     Layout l;
     l.off_imgs = align_up(sizeof(Ctrl), 256);
     l.off_tmaps = align_up(l.off_imgs + (size_t)n_imgs * sizeof(ImgDesc), 256);
     l.off_state = align_up(l.off_tmaps + (size_t)n_imgs * 2u * sizeof(CUtensorMap), 256);
     l.off_q0 = align_up(l.off_state + (size_t)G * 4u, 256);
     l.off_q1 = align_up(l.off_q0 + (size_t)cap * 4u, 256);
-    l.total = align_up(l.off_q1 + (two_queues ? (size_t)cap * 4u : 0u), 256);
+    l.off_sweep = align_up(l.off_q1 + (two_queues ? (size_t)cap * 4u : 0u), 256);
+    l.total = align_up(l.off_sweep + sweep_bytes, 256);
     return l;
 }
 
@@ -217,6 +219,19 @@ long long job_queue_capacity(const Job& job) {
     const long long req = job.cfg.queue_capacity < 0 ? -job.cfg.queue_capacity * std::max(job.G, 1ll)
                                                      : job.cfg.queue_capacity;
     return queue_capacity_for(job.variant, job.G, req);
+}
+
+// The workspace layout of a job (the same for direct calls and plans).
+Layout job_layout(const Job& job) {
+    const bool two = job.variant == IWPP_QUEUE_DOUBLE || job.variant == IWPP_QUEUE_UNIQUE;
+    size_t sweep = 0;
+    if (job.cfg.init_passes > 0)
+        for (const auto& d : job.descs) {
+            ImgDesc dv = d;
+            dv.conn = 4;
+            sweep = std::max(sweep, sweep_scratch_bytes(dv));
+        }
+    return layout_for((long long)job.descs.size(), job.G, job_queue_capacity(job), two, sweep);
 }
 
 // How images whose rows are not 4-byte aligned are handled.
@@ -487,7 +502,7 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
                 cudaEvent_t ev1, bool upload_descs, HostStaging* hs = nullptr) {
     const bool two = job.variant == IWPP_QUEUE_DOUBLE || job.variant == IWPP_QUEUE_UNIQUE;
     const long long cap = job_queue_capacity(job);
-    const Layout l = layout_for((long long)job.descs.size(), job.G, cap, two);
+    const Layout l = job_layout(job);
     int rc = ensure_workspace(ws, l.total);
     if (rc != IWPP_OK) return rc;
     char* base = static_cast<char*>(ws.base);
@@ -541,7 +556,7 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
                 static const int order[4] = {0, 1, 2, 3};
                 ImgDesc dv = d;
                 dv.conn = 4;
-                e = launch_sweep(dv, order[dir], s);
+                e = launch_sweep(dv, order[dir], s, base + l.off_sweep);
                 if (e != cudaSuccess) return cuda_status(e);
             }
     e = engine_launch_init(a, job.variant, s);
@@ -847,9 +862,7 @@ int iwpp_plan_create(iwpp_plan* out, iwpp_handle h, const iwpp_image* images, in
     }
     if (rc == IWPP_OK) {
         // Workspace and descriptors first (outside the graph, once).
-        const bool two = job.variant == IWPP_QUEUE_DOUBLE || job.variant == IWPP_QUEUE_UNIQUE;
-        const long long cap = job_queue_capacity(job);
-        const Layout l = layout_for((long long)job.descs.size(), job.G, cap, two);
+        const Layout l = job_layout(job);
         rc = ensure_workspace(p->ws, l.total);
         if (rc == IWPP_OK && !job.descs.empty()) {
             char* wbase = static_cast<char*>(p->ws.base);
@@ -1232,7 +1245,16 @@ int iwpp_sweep(void* marker, const void* mask, size_t pitch_marker, size_t pitch
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     iwpp_config c{};
     rc = build_job(job, &im, 1, IWPP_QUEUE_UNIQUE, &c, s, STAGE_ASYNC);
-    if (rc == IWPP_OK && !job.descs.empty()) rc = cuda_status(launch_sweep(job.descs[0], direction, s));
+    if (rc == IWPP_OK && !job.descs.empty()) {
+        void* scratch = nullptr;
+        const size_t sb = sweep_scratch_bytes(job.descs[0]);
+        if (sb > 0 && cudaMallocAsync(&scratch, sb, s) != cudaSuccess) {
+            cudaGetLastError();
+            scratch = nullptr;  // one warp per whole column instead
+        }
+        rc = cuda_status(launch_sweep(job.descs[0], direction, s, scratch));
+        if (scratch) cudaFreeAsync(scratch, s);
+    }
     const int rc2 = finish_staging(job, s);
     return set_last(rc == IWPP_OK ? rc2 : rc);
 }

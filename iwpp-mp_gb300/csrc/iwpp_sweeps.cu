@@ -379,8 +379,20 @@ constexpr int kRingN = 64;  // rows in flight per plane in the narrow variant
 // bytes per lane (uint8: two pixels as one u16x2 register; uint16: one
 // pixel), so the chain per row is one min and one max, and twice as many
 // warps share the image.
-template <int DT, bool DOWN>
-__global__ void __launch_bounds__(32) sweep_y4n_kernel(ImgDesc d) {
+//
+// Tall images are cut into segments of kSegRows rows so that more warps
+// share each column: the update of one column over a run of rows is
+// x -> max(min(x, B), A) for the value x entering the run (A = the run's
+// last value when nothing enters, B = the minimum of the mask over the run),
+// and such maps compose.  MODE 1 computes (A, B) per segment and column
+// without storing; sweep_y_carry_kernel chains them into the value entering
+// each segment; MODE 2 sweeps every segment from that value and stores.
+// MODE 0 is one warp over the whole column.
+constexpr int kSegRows = 1024;
+
+template <int DT, bool DOWN, int MODE>
+__global__ void __launch_bounds__(32) sweep_y4n_kernel(ImgDesc d, uint32_t* seg_a, uint32_t* seg_b,
+                                                       const uint32_t* seg_in) {
     static_assert(DT == DT_U8 || DT == DT_U16, "two-byte lanes");
     using P = Px<DT>;
     constexpr int NR = kRingN, NG = kRingN / kGroup;
@@ -391,10 +403,13 @@ __global__ void __launch_bounds__(32) sweep_y4n_kernel(ImgDesc d) {
     const long long row_bytes = (long long)d.W * P::BPP;
     const long long b0 = (long long)strip * 64 + lane * 2;  // this lane's first byte in a row
     const long long nbytes = row_bytes - b0;                 // >= 2: whole element, 1: half, <= 0: none
-    const int H = d.H;
+    // rows (in sweep order) of this block's segment
+    const int i0 = MODE == 0 ? 0 : (int)blockIdx.y * kSegRows;
+    const int H = MODE == 0 ? d.H : min(kSegRows, d.H - i0);
+    const size_t seg_idx = ((size_t)blockIdx.y * gridDim.x + strip) * 32 + lane;
     const long long step_m = DOWN ? d.pitch_m : -d.pitch_m, step_k = DOWN ? d.pitch_k : -d.pitch_k;
-    const unsigned char* m0 = d.marker + (size_t)(DOWN ? 0 : H - 1) * d.pitch_m;
-    const unsigned char* k0 = d.mask + (size_t)(DOWN ? 0 : H - 1) * d.pitch_k;
+    const unsigned char* m0 = d.marker + (size_t)(DOWN ? 0 : d.H - 1) * d.pitch_m + (long long)i0 * step_m;
+    const unsigned char* k0 = d.mask + (size_t)(DOWN ? 0 : d.H - 1) * d.pitch_k + (long long)i0 * step_k;
     const bool wide = (long long)(strip + 1) * 64 <= row_bytes &&
                       ((reinterpret_cast<uintptr_t>(d.marker) | reinterpret_cast<uintptr_t>(d.mask)) & 15u) == 0u &&
                       ((d.pitch_m | d.pitch_k) & 15) == 0;
@@ -433,7 +448,8 @@ __global__ void __launch_bounds__(32) sweep_y4n_kernel(ImgDesc d) {
         issue_group(g * kGroup);
         cp_async_commit();
     }
-    uint32_t prev = 0u;
+    uint32_t prev = MODE == 2 ? seg_in[seg_idx] : 0u;
+    uint32_t kmin = DT == DT_U8 ? 0x00ff00ffu : 0xffffu;
     unsigned char* mo = const_cast<unsigned char*>(m0) + (nbytes > 0 ? b0 : 0);
     for (int base = 0; base < H; base += kGroup) {
         cp_async_wait<NG - 1>();
@@ -443,31 +459,75 @@ __global__ void __launch_bounds__(32) sweep_y4n_kernel(ImgDesc d) {
 #pragma unroll
         for (int q = 0; q < kGroup; ++q) {
             uint32_t m = ring_m[sb + q][lane], k = ring_k[sb + q][lane];
+            const bool live = base + q < H;  // rows past the segment: stale slots
             if (DT == DT_U8) {
                 m = __byte_perm(m, 0u, 0x4140);
                 k = __byte_perm(k, 0u, 0x4140);
-                m = __vmaxu2(m, __vminu2(prev, k));
-                prev = m;
-                out[q] = __byte_perm(m, 0u, 0x0020);
+                const uint32_t v = __vmaxu2(m, __vminu2(prev, k));
+                if (MODE == 1) {
+                    if (live) {
+                        prev = v;
+                        kmin = __vminu2(kmin, k);
+                    }
+                } else {
+                    prev = v;
+                }
+                out[q] = __byte_perm(v, 0u, 0x0020);
             } else {
-                m = max(m, min(prev, k));
-                prev = m;
-                out[q] = m;
+                const uint32_t v = max(m, min(prev, k));
+                if (MODE == 1) {
+                    if (live) {
+                        prev = v;
+                        kmin = min(kmin, k);
+                    }
+                } else {
+                    prev = v;
+                }
+                out[q] = v;
             }
         }
-        if (nbytes >= 2) {
+        if (MODE != 1) {
+            if (nbytes >= 2) {
 #pragma unroll
-            for (int q = 0; q < kGroup; ++q)
-                if (base + q < H) *reinterpret_cast<uint16_t*>(mo + (long long)(base + q) * step_m) = (uint16_t)out[q];
-        } else if (nbytes == 1) {
-            for (int q = 0; q < kGroup; ++q)
-                if (base + q < H) *(mo + (long long)(base + q) * step_m) = (unsigned char)out[q];
+                for (int q = 0; q < kGroup; ++q)
+                    if (base + q < H)
+                        *reinterpret_cast<uint16_t*>(mo + (long long)(base + q) * step_m) = (uint16_t)out[q];
+            } else if (nbytes == 1) {
+                for (int q = 0; q < kGroup; ++q)
+                    if (base + q < H) *(mo + (long long)(base + q) * step_m) = (unsigned char)out[q];
+            }
         }
         __syncwarp();
         issue_group(base + NR);
         cp_async_commit();
     }
     cp_async_wait<0>();
+    if (MODE == 1) {
+        seg_a[seg_idx] = prev;
+        seg_b[seg_idx] = kmin;
+    }
+}
+
+// The value entering every segment of every column: x_0 = nothing (0),
+// x_{j+1} = max(min(x_j, B_j), A_j).  One thread per lane slot of a strip.
+template <int DT>
+__global__ void sweep_y_carry_kernel(int nseg, int slots, const uint32_t* seg_a, const uint32_t* seg_b,
+                                     uint32_t* seg_in) {
+    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (t >= slots) return;
+    uint32_t x = 0u;
+    for (int j = 0; j < nseg; ++j) {
+        const size_t idx = (size_t)j * slots + t;
+        seg_in[idx] = x;
+        x = DT == DT_U8 ? __vmaxu2(__vminu2(x, seg_b[idx]), seg_a[idx]) : max(min(x, seg_b[idx]), seg_a[idx]);
+    }
+}
+
+size_t sweep_scratch_bytes(const ImgDesc& d) {
+    if (d.dtype == DT_I32 || d.H <= 2 * kSegRows) return 0;
+    const long long strips = ((long long)d.W * (d.dtype == DT_U8 ? 1 : 2) + 63) / 64;
+    const long long nseg = (d.H + kSegRows - 1) / kSegRows;
+    return (size_t)(3 * nseg * strips * 32 * 4);
 }
 
 // ------------------------------------------------------------ host side
@@ -507,7 +567,7 @@ cudaError_t launch_clip(const ImgDesc& d, cudaStream_t s) {
 }
 
 template <int DT>
-static void launch_sweep_t(const ImgDesc& d, int direction, cudaStream_t s) {
+static void launch_sweep_t(const ImgDesc& d, int direction, cudaStream_t s, void* scratch) {
     using P = Px<DT>;
     constexpr int TW = 32 * P::PPW;
     if (direction == 0 || direction == 2) {
@@ -533,22 +593,40 @@ static void launch_sweep_t(const ImgDesc& d, int direction, cudaStream_t s) {
         } else {
             constexpr int NDT = DT == DT_I32 ? DT_U8 : DT;  // (never i32 here)
             const unsigned nblocks = (unsigned)(((long long)d.W * P::BPP + 63) / 64);
-            if (down)
-                sweep_y4n_kernel<NDT, true><<<nblocks, 32, 0, s>>>(d);
-            else
-                sweep_y4n_kernel<NDT, false><<<nblocks, 32, 0, s>>>(d);
+            if (scratch && sweep_scratch_bytes(d) > 0) {
+                // segments: aggregate, chain, sweep
+                const int nseg = (d.H + kSegRows - 1) / kSegRows;
+                const int slots = (int)nblocks * 32;
+                uint32_t* a = static_cast<uint32_t*>(scratch);
+                uint32_t* b = a + (size_t)nseg * slots;
+                uint32_t* in = b + (size_t)nseg * slots;
+                const dim3 grid(nblocks, (unsigned)nseg);
+                if (down)
+                    sweep_y4n_kernel<NDT, true, 1><<<grid, 32, 0, s>>>(d, a, b, nullptr);
+                else
+                    sweep_y4n_kernel<NDT, false, 1><<<grid, 32, 0, s>>>(d, a, b, nullptr);
+                sweep_y_carry_kernel<NDT><<<(unsigned)((slots + 127) / 128), 128, 0, s>>>(nseg, slots, a, b, in);
+                if (down)
+                    sweep_y4n_kernel<NDT, true, 2><<<grid, 32, 0, s>>>(d, nullptr, nullptr, in);
+                else
+                    sweep_y4n_kernel<NDT, false, 2><<<grid, 32, 0, s>>>(d, nullptr, nullptr, in);
+            } else if (down) {
+                sweep_y4n_kernel<NDT, true, 0><<<nblocks, 32, 0, s>>>(d, nullptr, nullptr, nullptr);
+            } else {
+                sweep_y4n_kernel<NDT, false, 0><<<nblocks, 32, 0, s>>>(d, nullptr, nullptr, nullptr);
+            }
         }
     }
 }
 
-cudaError_t launch_sweep(const ImgDesc& d, int direction, cudaStream_t s) {
+cudaError_t launch_sweep(const ImgDesc& d, int direction, cudaStream_t s, void* scratch) {
     if (d.W == 0 || d.H == 0) return cudaSuccess;
     if (d.dtype == DT_U8)
-        launch_sweep_t<DT_U8>(d, direction, s);
+        launch_sweep_t<DT_U8>(d, direction, s, scratch);
     else if (d.dtype == DT_U16)
-        launch_sweep_t<DT_U16>(d, direction, s);
+        launch_sweep_t<DT_U16>(d, direction, s, scratch);
     else
-        launch_sweep_t<DT_I32>(d, direction, s);
+        launch_sweep_t<DT_I32>(d, direction, s, scratch);
     return cudaGetLastError();
 }
 

@@ -214,6 +214,21 @@ def test_whole_image_sweeps_match_restatement(dt, conn):
         assert np.array_equal(from_dev(tm, NP[dt]), oracle.sweep(marker, mask, d, conn)), d
 
 
+@pytest.mark.parametrize("dt", [0, 1, 2])
+@pytest.mark.parametrize("shape", [(2500, 131), (4500, 64)])
+def test_vertical_sweeps_of_tall_images(dt, shape):
+    # more than two segments of rows: the segmented vertical sweep
+    torch = _torch()
+    h, w = shape
+    mask = synth.noise_mask(w, h, dt, 22, 3.0, 5)
+    marker = synth.sparse_marker(mask, 6, 0.001)
+    for d in (1, 3):
+        tm, tk = to_dev(marker), to_dev(mask)
+        iwpp.sweep(tm, tk, d, 4)
+        torch.cuda.synchronize()
+        assert np.array_equal(from_dev(tm, NP[dt]), oracle.sweep(marker, mask, d, 4)), d
+
+
 def test_sweep_timing_reports_four_passes():
     mask = synth.noise_mask(1024, 1024, 0, 1, 4.0, 50)
     marker = synth.hdome_marker(mask, 40)
