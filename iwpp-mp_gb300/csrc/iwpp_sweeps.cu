@@ -235,143 +235,13 @@ __global__ void __launch_bounds__(32) sweep_y_kernel(ImgDesc d) {
     cp_async_wait<0>();
 }
 
-// Vertical sweep for 4-connectivity (the whole-image init passes use it for
-// either connectivity: the pixel above / below alone is a valid update).
-// Same streaming as sweep_y_kernel, but the chain through the rows is two
-// SIMD operations per register: uint8 words are held as two u16x2 halves
-// (min / max on 16-bit pairs are single instructions), uint16 words are
-// u16x2 already, int32 is one signed pixel.  Stores are unconditional.
-template <int DT>
-struct Lanes4;
-template <>
-struct Lanes4<DT_U8> {
-    static constexpr int R = 2;  // registers per word
-    __device__ static __forceinline__ void split(uint32_t w, uint32_t (&r)[2]) {
-        r[0] = __byte_perm(w, 0u, 0x4140);  // pixels 0, 1 as u16x2
-        r[1] = __byte_perm(w, 0u, 0x4342);  // pixels 2, 3
-    }
-    __device__ static __forceinline__ uint32_t join(const uint32_t (&r)[2]) { return __byte_perm(r[0], r[1], 0x6420); }
-    __device__ static __forceinline__ uint32_t mn(uint32_t a, uint32_t b) { return __vminu2(a, b); }
-    __device__ static __forceinline__ uint32_t mx(uint32_t a, uint32_t b) { return __vmaxu2(a, b); }
-    static constexpr uint32_t MIN = 0u;
-};
-template <>
-struct Lanes4<DT_U16> {
-    static constexpr int R = 1;
-    __device__ static __forceinline__ void split(uint32_t w, uint32_t (&r)[1]) { r[0] = w; }
-    __device__ static __forceinline__ uint32_t join(const uint32_t (&r)[1]) { return r[0]; }
-    __device__ static __forceinline__ uint32_t mn(uint32_t a, uint32_t b) { return __vminu2(a, b); }
-    __device__ static __forceinline__ uint32_t mx(uint32_t a, uint32_t b) { return __vmaxu2(a, b); }
-    static constexpr uint32_t MIN = 0u;
-};
-template <>
-struct Lanes4<DT_I32> {
-    static constexpr int R = 1;
-    __device__ static __forceinline__ void split(uint32_t w, uint32_t (&r)[1]) { r[0] = w; }
-    __device__ static __forceinline__ uint32_t join(const uint32_t (&r)[1]) { return r[0]; }
-    __device__ static __forceinline__ uint32_t mn(uint32_t a, uint32_t b) { return (uint32_t)min((int)a, (int)b); }
-    __device__ static __forceinline__ uint32_t mx(uint32_t a, uint32_t b) { return (uint32_t)max((int)a, (int)b); }
-    static constexpr uint32_t MIN = 0x80000000u;
-};
-
-template <int DT, bool DOWN>
-__global__ void __launch_bounds__(32) sweep_y4_kernel(ImgDesc d) {
-    using P = Px<DT>;
-    using L = Lanes4<DT>;
-    constexpr int TW = 32 * P::PPW;
-    constexpr int R = L::R;
-    constexpr int NG = kRing / kGroup;
-    __shared__ __align__(16) uint32_t ring_m[kRing][32];
-    __shared__ __align__(16) uint32_t ring_k[kRing][32];
-    const int lane = threadIdx.x & 31;
-    const int strip = (int)blockIdx.x;
-    const int px0 = strip * TW + lane * P::PPW, npx = d.W - px0;
-    const size_t off = (size_t)(npx > 0 ? px0 : 0) * P::BPP;
-    const int H = d.H;
-    const long long step_m = DOWN ? d.pitch_m : -d.pitch_m, step_k = DOWN ? d.pitch_k : -d.pitch_k;
-    const unsigned char* m0 = d.marker + (size_t)(DOWN ? 0 : H - 1) * d.pitch_m + off;
-    const unsigned char* k0 = d.mask + (size_t)(DOWN ? 0 : H - 1) * d.pitch_k + off;
-    // Whole 128-byte rows of the strip in 16-byte pieces (lane = piece of a
-    // row: 8 pieces per row and plane, 4 rows per instruction) when the
-    // strip lies inside every row and both planes are 16-byte aligned;
-    // otherwise one 4-byte word per lane and row.
-    const unsigned char* sm0 = d.marker + (size_t)(DOWN ? 0 : H - 1) * d.pitch_m + (size_t)strip * 128u;
-    const unsigned char* sk0 = d.mask + (size_t)(DOWN ? 0 : H - 1) * d.pitch_k + (size_t)strip * 128u;
-    const bool wide = (long long)(strip + 1) * 128 <= (long long)d.W * P::BPP &&
-                      ((reinterpret_cast<uintptr_t>(d.marker) | reinterpret_cast<uintptr_t>(d.mask)) & 15u) == 0u &&
-                      ((d.pitch_m | d.pitch_k) & 15) == 0;
-    auto issue_group = [&](int g0) {  // rows g0 .. g0 + kGroup - 1 (those below H)
-        if (wide) {
-            const int piece = lane & 7;
-#pragma unroll
-            for (int rr = 0; rr < kGroup; rr += 4) {
-                const int i = g0 + rr + (lane >> 3);
-                if (i < H) {
-                    const int slot = i % kRing;
-                    cp_async16(&ring_m[slot][piece * 4], sm0 + (long long)i * step_m + piece * 16);
-                    cp_async16(&ring_k[slot][piece * 4], sk0 + (long long)i * step_k + piece * 16);
-                }
-            }
-        } else {
-            for (int q = 0; q < kGroup; ++q) {
-                const int i = g0 + q;
-                if (i >= H) break;
-                const int slot = i % kRing;
-                const unsigned char* mrow = m0 + (long long)i * step_m;
-                const unsigned char* krow = k0 + (long long)i * step_k;
-                if (npx >= P::PPW) {
-                    cp_async4(&ring_m[slot][lane], mrow);
-                    cp_async4(&ring_k[slot][lane], krow);
-                } else {
-                    uint32_t mw = P::MINW, kw = P::MINW;
-                    if (npx > 0) load_pair<DT>(mrow, krow, npx, mw, kw);
-                    ring_m[slot][lane] = mw;
-                    ring_k[slot][lane] = kw;
-                }
-            }
-        }
-    };
-    for (int g = 0; g < NG; ++g) {
-        issue_group(g * kGroup);
-        cp_async_commit();
-    }
-    uint32_t prev[R];
-#pragma unroll
-    for (int j = 0; j < R; ++j) prev[j] = L::MIN;
-    for (int base = 0; base < H; base += kGroup) {
-        cp_async_wait<NG - 1>();
-        __syncwarp();  // pieces copied by other lanes are visible to this one
-        const int sb = base % kRing;
-        uint32_t out[kGroup];
-#pragma unroll
-        for (int q = 0; q < kGroup; ++q) {
-            uint32_t m[R], k[R];
-            L::split(ring_m[sb + q][lane], m);
-            L::split(ring_k[sb + q][lane], k);
-#pragma unroll
-            for (int j = 0; j < R; ++j) {
-                m[j] = L::mx(m[j], L::mn(prev[j], k[j]));
-                prev[j] = m[j];
-            }
-            out[q] = L::join(m);
-        }
-        if (npx >= P::PPW) {
-#pragma unroll
-            for (int q = 0; q < kGroup; ++q)
-                if (base + q < H)
-                    *reinterpret_cast<uint32_t*>(const_cast<unsigned char*>(m0) + (long long)(base + q) * step_m) =
-                        out[q];
-        } else if (npx > 0) {
-            for (int q = 0; q < kGroup; ++q)
-                if (base + q < H)
-                    store_word_plain<DT>(const_cast<unsigned char*>(m0) + (long long)(base + q) * step_m, npx, out[q]);
-        }
-        __syncwarp();  // the slots just read are refilled next
-        issue_group(base + kRing);
-        cp_async_commit();
-    }
-    cp_async_wait<0>();
-}
+// Vertical sweep for 4-connectivity, int32 (the whole-image init passes use
+// the 4-connected vertical sweeps for either connectivity: the pixel above /
+// below alone is a valid update).  One pixel per lane, 128-byte strips,
+// segments and modes as in sweep_y4n_kernel below.
+template <bool DOWN, int MODE>
+__global__ void __launch_bounds__(32) sweep_y4i_kernel(ImgDesc d, uint32_t* seg_a, uint32_t* seg_b,
+                                                       const uint32_t* seg_in);
 
 constexpr int kRingN = 64;  // rows in flight per plane in the narrow variant
 
@@ -508,6 +378,95 @@ __global__ void __launch_bounds__(32) sweep_y4n_kernel(ImgDesc d, uint32_t* seg_
     }
 }
 
+template <bool DOWN, int MODE>
+__global__ void __launch_bounds__(32) sweep_y4i_kernel(ImgDesc d, uint32_t* seg_a, uint32_t* seg_b,
+                                                       const uint32_t* seg_in) {
+    constexpr int NG = kRing / kGroup;
+    __shared__ __align__(16) uint32_t ring_m[kRing][32];
+    __shared__ __align__(16) uint32_t ring_k[kRing][32];
+    const int lane = threadIdx.x & 31;
+    const int strip = (int)blockIdx.x;
+    const int x = strip * 32 + lane;
+    const bool inside = x < d.W;
+    const int i0 = MODE == 0 ? 0 : (int)blockIdx.y * kSegRows;
+    const int H = MODE == 0 ? d.H : min(kSegRows, d.H - i0);
+    const size_t seg_idx = ((size_t)blockIdx.y * gridDim.x + strip) * 32 + lane;
+    const long long step_m = DOWN ? d.pitch_m : -d.pitch_m, step_k = DOWN ? d.pitch_k : -d.pitch_k;
+    const unsigned char* m0 = d.marker + (size_t)(DOWN ? 0 : d.H - 1) * d.pitch_m + (long long)i0 * step_m;
+    const unsigned char* k0 = d.mask + (size_t)(DOWN ? 0 : d.H - 1) * d.pitch_k + (long long)i0 * step_k;
+    const long long sbase = (long long)strip * 128;
+    const bool wide = (long long)(strip + 1) * 32 <= (long long)d.W &&
+                      ((reinterpret_cast<uintptr_t>(d.marker) | reinterpret_cast<uintptr_t>(d.mask)) & 15u) == 0u &&
+                      ((d.pitch_m | d.pitch_k) & 15) == 0;
+    auto issue_group = [&](int g0) {
+        if (wide) {  // 8 pieces of 16 bytes per row and plane, 4 rows per instruction
+            const int piece = lane & 7;
+#pragma unroll
+            for (int rr = 0; rr < kGroup; rr += 4) {
+                const int i = g0 + rr + (lane >> 3);
+                if (i < H) {
+                    const int slot = i % kRing;
+                    cp_async16(&ring_m[slot][piece * 4], m0 + (long long)i * step_m + sbase + piece * 16);
+                    cp_async16(&ring_k[slot][piece * 4], k0 + (long long)i * step_k + sbase + piece * 16);
+                }
+            }
+        } else {
+            for (int q = 0; q < kGroup; ++q) {
+                const int i = g0 + q;
+                if (i >= H) break;
+                const int slot = i % kRing;
+                uint32_t mv = 0x80000000u, kv = 0x80000000u;
+                if (inside) {
+                    mv = *reinterpret_cast<const uint32_t*>(m0 + (long long)i * step_m + (long long)x * 4);
+                    kv = *reinterpret_cast<const uint32_t*>(k0 + (long long)i * step_k + (long long)x * 4);
+                }
+                ring_m[slot][lane] = mv;
+                ring_k[slot][lane] = kv;
+            }
+        }
+    };
+    for (int g = 0; g < NG; ++g) {
+        issue_group(g * kGroup);
+        cp_async_commit();
+    }
+    int prev = MODE == 2 ? (int)seg_in[seg_idx] : INT_MIN;
+    int kmin = INT_MAX;
+    unsigned char* mo = const_cast<unsigned char*>(m0) + (long long)(inside ? x : 0) * 4;
+    for (int base = 0; base < H; base += kGroup) {
+        cp_async_wait<NG - 1>();
+        __syncwarp();  // pieces copied by other lanes are visible to this one
+        const int sb = base % kRing;
+        int out[kGroup];
+#pragma unroll
+        for (int q = 0; q < kGroup; ++q) {
+            const int m = (int)ring_m[sb + q][lane], k = (int)ring_k[sb + q][lane];
+            const int v = max(m, min(prev, k));
+            if (MODE == 1) {
+                if (base + q < H) {  // rows past the segment: stale slots
+                    prev = v;
+                    kmin = min(kmin, k);
+                }
+            } else {
+                prev = v;
+            }
+            out[q] = v;
+        }
+        if (MODE != 1 && inside) {
+#pragma unroll
+            for (int q = 0; q < kGroup; ++q)
+                if (base + q < H) *reinterpret_cast<int*>(mo + (long long)(base + q) * step_m) = out[q];
+        }
+        __syncwarp();  // the slots just read are refilled next
+        issue_group(base + kRing);
+        cp_async_commit();
+    }
+    cp_async_wait<0>();
+    if (MODE == 1) {
+        seg_a[seg_idx] = (uint32_t)prev;
+        seg_b[seg_idx] = (uint32_t)kmin;
+    }
+}
+
 // The value entering every segment of every column: x_0 = nothing (0),
 // x_{j+1} = max(min(x_j, B_j), A_j).  One thread per lane slot of a strip.
 template <int DT>
@@ -515,17 +474,23 @@ __global__ void sweep_y_carry_kernel(int nseg, int slots, const uint32_t* seg_a,
                                      uint32_t* seg_in) {
     const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (t >= slots) return;
-    uint32_t x = 0u;
+    uint32_t x = DT == DT_I32 ? 0x80000000u : 0u;
     for (int j = 0; j < nseg; ++j) {
         const size_t idx = (size_t)j * slots + t;
         seg_in[idx] = x;
-        x = DT == DT_U8 ? __vmaxu2(__vminu2(x, seg_b[idx]), seg_a[idx]) : max(min(x, seg_b[idx]), seg_a[idx]);
+        if (DT == DT_U8)
+            x = __vmaxu2(__vminu2(x, seg_b[idx]), seg_a[idx]);
+        else if (DT == DT_U16)
+            x = max(min(x, seg_b[idx]), seg_a[idx]);
+        else
+            x = (uint32_t)max(min((int)x, (int)seg_b[idx]), (int)seg_a[idx]);
     }
 }
 
 size_t sweep_scratch_bytes(const ImgDesc& d) {
-    if (d.dtype == DT_I32 || d.H <= 2 * kSegRows) return 0;
-    const long long strips = ((long long)d.W * (d.dtype == DT_U8 ? 1 : 2) + 63) / 64;
+    if (d.conn != 4 || d.H <= 2 * kSegRows) return 0;
+    const long long strips = d.dtype == DT_I32 ? ((long long)d.W + 31) / 32
+                                               : ((long long)d.W * (d.dtype == DT_U8 ? 1 : 2) + 63) / 64;
     const long long nseg = (d.H + kSegRows - 1) / kSegRows;
     return (size_t)(3 * nseg * strips * 32 * 4);
 }
@@ -586,10 +551,28 @@ static void launch_sweep_t(const ImgDesc& d, int direction, cudaStream_t s, void
             else
                 sweep_y_kernel<DT, 8, false><<<blocks, 32, 0, s>>>(d);
         } else if (DT == DT_I32) {
-            if (down)
-                sweep_y4_kernel<DT, true><<<blocks, 32, 0, s>>>(d);
-            else
-                sweep_y4_kernel<DT, false><<<blocks, 32, 0, s>>>(d);
+            const unsigned nblocks = (unsigned)((d.W + 31) / 32);
+            if (scratch && sweep_scratch_bytes(d) > 0) {
+                const int nseg = (d.H + kSegRows - 1) / kSegRows;
+                const int slots = (int)nblocks * 32;
+                uint32_t* a = static_cast<uint32_t*>(scratch);
+                uint32_t* b = a + (size_t)nseg * slots;
+                uint32_t* in = b + (size_t)nseg * slots;
+                const dim3 grid(nblocks, (unsigned)nseg);
+                if (down)
+                    sweep_y4i_kernel<true, 1><<<grid, 32, 0, s>>>(d, a, b, nullptr);
+                else
+                    sweep_y4i_kernel<false, 1><<<grid, 32, 0, s>>>(d, a, b, nullptr);
+                sweep_y_carry_kernel<DT_I32><<<(unsigned)((slots + 127) / 128), 128, 0, s>>>(nseg, slots, a, b, in);
+                if (down)
+                    sweep_y4i_kernel<true, 2><<<grid, 32, 0, s>>>(d, nullptr, nullptr, in);
+                else
+                    sweep_y4i_kernel<false, 2><<<grid, 32, 0, s>>>(d, nullptr, nullptr, in);
+            } else if (down) {
+                sweep_y4i_kernel<true, 0><<<nblocks, 32, 0, s>>>(d, nullptr, nullptr, nullptr);
+            } else {
+                sweep_y4i_kernel<false, 0><<<nblocks, 32, 0, s>>>(d, nullptr, nullptr, nullptr);
+            }
         } else {
             constexpr int NDT = DT == DT_I32 ? DT_U8 : DT;  // (never i32 here)
             const unsigned nblocks = (unsigned)(((long long)d.W * P::BPP + 63) / 64);
