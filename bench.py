@@ -570,6 +570,16 @@ def run_ours(args):
         torch.distributed.barrier()
     value = whole_job_gpx(world, px_step, args.steps, elapsed_ms)
 
+    # ---- serving sub-result first: the host-to-device path of a shared box
+    # slows down for a while after heavy copy traffic such as the end-to-end
+    # legs below
+    served = None
+    if rank == 0 and not args.no_extras:
+        try:
+            served = bench_served(args, dev, variant)
+        except Exception as exc:  # reported in the line, the headline stands
+            served = {"error": f"{type(exc).__name__}: {exc}"}
+
     # ---- end to end: pinned host buffers in, host buffers out, every copy
     # inside the timed region.  `e2e`: each image through the per-image C-ABI
     # call (iwpp_reconstruct_async) with its H2D and D2H copies on their own
@@ -625,6 +635,8 @@ def run_ours(args):
                 if st != 0:
                     raise iwpp.IwppError(st, "iwpp_handle_sync")
 
+        e2e_steps_used = min(args.steps, 60)  # bounded copy volume; the rate is per step
+
         def timed(step_fn, overlap_steps):
             for _ in range(max(args.warmup, 3)):
                 step_fn()
@@ -633,22 +645,23 @@ def run_ours(args):
                 o.zero_()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            for k in range(args.steps):
+            for k in range(e2e_steps_used):
                 if overlap_steps:
-                    step_fn(finish=k == args.steps - 1)
+                    step_fn(finish=k == e2e_steps_used - 1)
                 else:
                     step_fn()
             secs = time.perf_counter() - t0
             ok = ok and all(np.array_equal(host_out[i].numpy(), results[i]) for i in range(len(cases)))
-            return world * px_step * args.steps / secs / 1e9, ok
+            return world * px_step * e2e_steps_used / secs / 1e9, ok
 
         sync_value, sync_ok = timed(sync_step, False)
         pipe_value, pipe_ok = timed(pipelined_step, True)
+        e2e_steps = e2e_steps_used
         e2e = {"value": pipe_value, "unit": UNIT,
                "h2d_bytes_per_step": len(cases) * 2 * W * H, "d2h_bytes_per_step": len(cases) * W * H,
                "path": "iwpp_reconstruct_async per image, H2D / reconstruction / D2H on three streams, "
                        "steps back to back (one host wait at the end of the timed region)",
-               "bitexact_vs_device_path": pipe_ok,
+               "bitexact_vs_device_path": pipe_ok, "steps": e2e_steps,
                "sync_call": {"value": sync_value, "unit": UNIT, "bitexact_vs_device_path": sync_ok,
                              "path": "synchronous iwpp_reconstruct per image, copies before and after"}}
 
@@ -680,8 +693,10 @@ def run_ours(args):
         "gpu_launches": args.steps * len(cases) * 2,
     }
     handle.close()
+    if served is not None:
+        line["served"] = served
     if not args.no_extras:
-        for key, fn in (("served", bench_served), ("batched", bench_batched), ("spiral", bench_spiral)):
+        for key, fn in (("batched", bench_batched), ("spiral", bench_spiral)):
             try:
                 line[key] = fn(args, dev, variant)
             except Exception as exc:  # reported in the line, the headline stands

@@ -487,8 +487,11 @@ __global__ void sweep_y_carry_kernel(int nseg, int slots, const uint32_t* seg_a,
     }
 }
 
+// int32 is not segmented: at four bytes a pixel the two extra plane reads
+// cost more than the parallelism gains (its strips already give 512 warps
+// on a 16384-wide image).
 size_t sweep_scratch_bytes(const ImgDesc& d) {
-    if (d.conn != 4 || d.H <= 2 * kSegRows) return 0;
+    if (d.conn != 4 || d.dtype == DT_I32 || d.H <= 2 * kSegRows) return 0;
     const long long strips = d.dtype == DT_I32 ? ((long long)d.W + 31) / 32
                                                : ((long long)d.W * (d.dtype == DT_U8 ? 1 : 2) + 63) / 64;
     const long long nseg = (d.H + kSegRows - 1) / kSegRows;
