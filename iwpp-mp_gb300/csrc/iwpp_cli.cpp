@@ -16,7 +16,9 @@
 // options: --conn 4|8 (default 4, the reference's), --variant
 // mutex|double|unique|async|default, --raw WxH:u8|u16|i32 (how to read .raw
 // inputs), --no-clip, --repeat N (time N runs from the same marker, report
-// the median), --convert IN OUT (I/O only, no GPU: rewrite IN as OUT).
+// the median), --init-passes N, --solver 0|1|2, --tile-rows 32|64 (the
+// iwpp_config fields; default: the library's defaults), --convert IN OUT
+// (I/O only, no GPU: rewrite IN as OUT).
 #include <algorithm>
 #include <cctype>
 #include <chrono>
@@ -291,6 +293,7 @@ int usage() {
     std::fprintf(stderr,
                  "usage: iwpp_cli <marker> <mask> <output> <usePGMLoader> [--conn 4|8] [--variant V]\n"
                  "                [--raw WxH:u8|u16|i32] [--no-clip] [--repeat N]\n"
+                 "                [--init-passes N] [--solver 0|1|2] [--tile-rows 32|64]\n"
                  "       iwpp_cli --convert <in> <out> [--raw WxH:type]\n");
     return 1;
 }
@@ -300,6 +303,8 @@ int usage() {
 int main(int argc, char** argv) {
     std::vector<std::string> pos;
     int conn = 4, variant = IWPP_QUEUE_DEFAULT, repeat = 1;
+    iwpp_config cfg{};
+    cfg.init_passes = -1;
     bool clip = true, convert = false;
     std::string raw_spec;
     for (int i = 1; i < argc; ++i) {
@@ -312,6 +317,12 @@ int main(int argc, char** argv) {
                     : v == "unique" ? IWPP_QUEUE_UNIQUE : v == "async" ? IWPP_QUEUE_ASYNC : IWPP_QUEUE_DEFAULT;
         } else if (a == "--raw" && i + 1 < argc) {
             raw_spec = argv[++i];
+        } else if (a == "--init-passes" && i + 1 < argc) {
+            cfg.init_passes = std::atoi(argv[++i]);
+        } else if (a == "--solver" && i + 1 < argc) {
+            cfg.solver = std::atoi(argv[++i]);
+        } else if (a == "--tile-rows" && i + 1 < argc) {
+            cfg.tile_rows = std::atoi(argv[++i]);
         } else if (a == "--no-clip") {
             clip = false;
         } else if (a == "--repeat" && i + 1 < argc) {
@@ -362,7 +373,7 @@ int main(int argc, char** argv) {
             cudaMemcpy2D(d_marker, pm, d_pristine, pp, row, (size_t)marker.h, cudaMemcpyDeviceToDevice);
         cudaDeviceSynchronize();
         const auto t0 = std::chrono::high_resolution_clock::now();
-        rc = iwpp_reconstruct(h, d_marker, d_mask, pm, pk, marker.w, marker.h, marker.dtype, conn, variant, nullptr,
+        rc = iwpp_reconstruct(h, d_marker, d_mask, pm, pk, marker.w, marker.h, marker.dtype, conn, variant, &cfg,
                               nullptr, nullptr);
         const auto t1 = std::chrono::high_resolution_clock::now();
         times.push_back(std::chrono::duration<double, std::milli>(t1 - t0).count());

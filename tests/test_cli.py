@@ -98,7 +98,7 @@ def test_reconstruction_uint16_tiff_and_unclipped_marker(cli, tmp_path):
     write_pgm(tmp_path / "marker.pgm", marker)
     write_pgm(tmp_path / "mask.pgm", mask)
     r = run(cli, tmp_path / "marker.pgm", tmp_path / "mask.pgm", tmp_path / "out.tif", 0, "--conn", 8,
-            "--variant", "unique", "--repeat", 3)
+            "--variant", "unique", "--repeat", 3, "--init-passes", 2, "--solver", 2, "--tile-rows", 32)
     assert r.returncode == 0, r.stderr
     assert run(cli, "--convert", tmp_path / "out.tif", tmp_path / "out.raw").returncode == 0
     out = read_raw(tmp_path / "out.raw", mask.shape, np.uint16)
