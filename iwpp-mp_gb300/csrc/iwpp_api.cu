@@ -1262,21 +1262,42 @@ int iwpp_sweep(void* marker, const void* mask, size_t pitch_marker, size_t pitch
 int iwpp_sweep_timing(void* marker, const void* mask, size_t pitch_marker, size_t pitch_mask, int width,
                       int height, int dtype, int connectivity, float* ms_out) {
     if (!ms_out) return set_last(IWPP_ERR_INVALID);
-    cudaEvent_t ev[5];
-    for (auto& e : ev) cudaEventCreate(&e);
-    int rc = IWPP_OK;
-    cudaEventRecord(ev[0], nullptr);
-    for (int dir = 0; dir < 4 && rc == IWPP_OK; ++dir) {
-        rc = iwpp_sweep(marker, mask, pitch_marker, pitch_mask, width, height, dtype, connectivity, dir, nullptr);
-        cudaEventRecord(ev[dir + 1], nullptr);
+    int rc = check_image(marker, mask, pitch_marker, pitch_mask, width, height, dtype, connectivity);
+    if (rc != IWPP_OK) return set_last(rc);
+    for (int dir = 0; dir < 4; ++dir) ms_out[dir] = 0.f;
+    if (width == 0 || height == 0) return set_last(IWPP_OK);
+    // Prepared once (staging, scratch), then the four kernels alone between
+    // events, as the reference times its passes (DQ MR.cu:1077-1178).
+    iwpp_image im{marker, mask, pitch_marker, pitch_mask, width, height, dtype, connectivity};
+    Job job;
+    cudaStream_t s = nullptr;
+    iwpp_config c{};
+    rc = build_job(job, &im, 1, IWPP_QUEUE_UNIQUE, &c, s, STAGE_ASYNC);
+    void* scratch = nullptr;
+    cudaEvent_t ev[5] = {};
+    if (rc == IWPP_OK && !job.descs.empty()) {
+        const size_t sb = sweep_scratch_bytes(job.descs[0]);
+        if (sb > 0 && cudaMallocAsync(&scratch, sb, s) != cudaSuccess) {
+            cudaGetLastError();
+            scratch = nullptr;
+        }
+        for (auto& e : ev) cudaEventCreate(&e);
+        cudaEventRecord(ev[0], s);
+        for (int dir = 0; dir < 4 && rc == IWPP_OK; ++dir) {
+            rc = cuda_status(launch_sweep(job.descs[0], dir, s, scratch));
+            cudaEventRecord(ev[dir + 1], s);
+        }
+        if (rc == IWPP_OK) {
+            rc = cuda_status(cudaEventSynchronize(ev[4]));
+            for (int dir = 0; dir < 4 && rc == IWPP_OK; ++dir) cudaEventElapsedTime(&ms_out[dir], ev[dir], ev[dir + 1]);
+        }
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+        if (scratch) cudaFreeAsync(scratch, s);
     }
-    if (rc == IWPP_OK) {
-        cudaError_t e = cudaEventSynchronize(ev[4]);
-        rc = cuda_status(e);
-        for (int dir = 0; dir < 4 && rc == IWPP_OK; ++dir) cudaEventElapsedTime(&ms_out[dir], ev[dir], ev[dir + 1]);
-    }
-    for (auto& e : ev) cudaEventDestroy(e);
-    return set_last(rc);
+    const int rc2 = finish_staging(job, s);
+    cudaStreamSynchronize(s);
+    return set_last(rc == IWPP_OK ? rc2 : rc);
 }
 
 void MorphologicalReconstruction(unsigned char* marker, unsigned char* mask, size_t pitchMarker, size_t pitchMask,
