@@ -56,7 +56,8 @@ typedef enum iwpp_queue_variant {
  * init_passes -1, solver 0; or cfg NULL) are taken from the tuning table
  * when it holds an entry for the job's workload class (iwpp_autotune). */
 typedef struct iwpp_config {
-    int tile_rows;             /* 32 or 64 rows per tile; 0 = default (64) */
+    int tile_rows;             /* 32 or 64 rows per tile; 0 = default: 64, or 32 when the
+                                  job has fewer than four 64-row tiles per resident warp */
     long long queue_capacity;  /* entries per queue buffer; 0 = default; < 0: that multiple
                                   of the job's tile count */
     int init_passes;           /* whole-image passes first (+X, +Y, -X, -Y each); -1 = default (0) */
@@ -114,7 +115,8 @@ IWPP_API int iwpp_handle_create(iwpp_handle *out, int device);
 IWPP_API int iwpp_handle_destroy(iwpp_handle h);
 /* Bytes of device workspace a job of `tiles` tiles needs. */
 IWPP_API long long iwpp_workspace_bytes(long long tiles, int variant, long long queue_capacity);
-/* Tiles of one image for a dtype and tile height (0 = default). */
+/* Tiles of one image for a dtype and tile height (0 = the default height a
+ * single-image call on the current device picks). */
 IWPP_API long long iwpp_tile_count(int width, int height, int dtype, int tile_rows);
 
 /* ---- plain reconstruction (replaces MorphologicalReconstruction,

@@ -96,7 +96,8 @@ namespace {
 // planes, its share of the tile-state words and queue ring, its descriptor.
 size_t request_bytes(int w, int h, int dtype, int tile_rows, size_t* pitch_out) {
     const size_t pitch = round_up((size_t)w * (size_t)bpp_of(dtype), 128);
-    const long long tiles = iwpp_tile_count(w, h, dtype, tile_rows);
+    // a batch may pick either tile height when none is set: count the smaller
+    const long long tiles = iwpp_tile_count(w, h, dtype, tile_rows ? tile_rows : 32);
     *pitch_out = pitch;
     return 2 * pitch * (size_t)h + (size_t)std::max(0ll, tiles) * 16u + 1024u;
 }
@@ -245,8 +246,9 @@ int iwpp_server_create(iwpp_server* out, int device, const iwpp_server_config* c
         unsigned long long keep = ~0ull;
         e = cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
     }
-    // Each lane's workspace is sized once for the most tiles the budget can admit.
-    const int th = c.tile_rows ? c.tile_rows : 64;
+    // Each lane's workspace is sized once for the most tiles the budget can
+    // admit: with the tile height left to each batch, its smaller choice.
+    const int th = c.tile_rows ? c.tile_rows : 32;
     const long long max_tiles = std::max(1ll, s->budget / (2ll * 128ll * th));
     const long long ws_bytes =
         iwpp_workspace_bytes(max_tiles, s->variant, 0) + (long long)s->max_batch * 512ll + 4096ll;

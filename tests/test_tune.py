@@ -82,6 +82,15 @@ def _host(t, dtype):
 
 
 @pytest.mark.gpu
+def test_default_tile_height_follows_the_tile_count():
+    iwpp.tune_clear()
+    # 88 tiles of 64 rows: fewer than the device keeps warps resident
+    assert iwpp.tile_count(1000, 700, 0, 0) == iwpp.tile_count(1000, 700, 0, 32)
+    # 65536 tiles of 64 rows: more than four per warp any device keeps resident
+    assert iwpp.tile_count(32768, 16384, 0, 0) == iwpp.tile_count(32768, 16384, 0, 64)
+
+
+@pytest.mark.gpu
 def test_table_entry_steers_default_calls(tmp_path):
     iwpp.tune_clear()
     mask = synth.noise_mask(1000, 700, 0, 31, 3.0, 5)
@@ -91,18 +100,18 @@ def test_table_entry_steers_default_calls(tmp_path):
     t32 = iwpp.tile_count(1000, 700, 0, 32)
     m, k = _dev(marker), _dev(mask)
     st = iwpp.reconstruct(m, k, connectivity=8, variant="async")
-    assert st.tiles == t64 and np.array_equal(_host(m, marker.dtype), ref)
+    assert st.tiles == t32 and np.array_equal(_host(m, marker.dtype), ref)
     cls = (1000 * 700).bit_length() - 1
     p = tmp_path / "t.txt"
-    _write(p, [f"3 0 8 {cls} 0 32 2 1 0"])
+    _write(p, [f"3 0 8 {cls} 0 64 2 1 0"])
     iwpp.tune_load(str(p))
     m, k = _dev(marker), _dev(mask)
     st = iwpp.reconstruct(m, k, connectivity=8, variant="async")
-    assert st.tiles == t32 and np.array_equal(_host(m, marker.dtype), ref)
+    assert st.tiles == t64 and np.array_equal(_host(m, marker.dtype), ref)
     # explicit fields win over the table
     m, k = _dev(marker), _dev(mask)
-    st = iwpp.reconstruct(m, k, connectivity=8, variant="async", config=iwpp.Config.make(tile_rows=64))
-    assert st.tiles == t64 and np.array_equal(_host(m, marker.dtype), ref)
+    st = iwpp.reconstruct(m, k, connectivity=8, variant="async", config=iwpp.Config.make(tile_rows=32))
+    assert st.tiles == t32 and np.array_equal(_host(m, marker.dtype), ref)
     iwpp.tune_clear()
 
 
