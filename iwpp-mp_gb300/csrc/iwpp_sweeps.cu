@@ -98,6 +98,15 @@ __global__ void fixed_point_kernel(ImgDesc d, unsigned long long* count) {
 }
 
 // --------------------------------------------------------------- X sweeps
+// Chunks a warp keeps in flight ahead of the one it scans: the row's loads
+// do not depend on the carry, so they are issued kXAhead chunks early into a
+// register ring (the walk is otherwise one global-memory latency per chunk).
+// A chunk is loaded before any store of this warp to it, and no other warp
+// touches the row, so no load reads a value this sweep has replaced.
+// Measured on 16384^2 rows: 2 ahead takes 14-24 % off a uint8 / uint16
+// sweep and 5 % off int32; 4 or 8 ahead gain less (int32: lose).
+constexpr int kXAhead = 2;
+
 template <int DT, bool FWD>
 __global__ void sweep_x_kernel(ImgDesc d) {
     using P = Px<DT>;
@@ -108,19 +117,36 @@ __global__ void sweep_x_kernel(ImgDesc d) {
     const int chunks = (d.W + TW - 1) / TW;
     unsigned char* mbase = d.marker + (size_t)row * d.pitch_m;
     const unsigned char* kbase = d.mask + (size_t)row * d.pitch_k;
-    uint32_t carry = P::MINPX;
-    for (int cc = 0; cc < chunks; ++cc) {
-        const int c = FWD ? cc : chunks - 1 - cc;
-        const int px0 = c * TW + lane * P::PPW, npx = d.W - px0;
-        uint32_t mw = P::MINW, kw = P::MINW;
+    // chunk cc in walk order: its first pixel for this lane and how many of
+    // the lane's pixels lie inside the row
+    auto px0_of = [&](int cc) { return (FWD ? cc : chunks - 1 - cc) * TW + lane * P::PPW; };
+    auto fetch = [&](int cc, uint32_t& mw, uint32_t& kw) {
+        mw = P::MINW;
+        kw = P::MINW;
+        if (cc >= chunks) return;
+        const int px0 = px0_of(cc), npx = d.W - px0;
         if (npx > 0) load_pair<DT>(mbase + (size_t)px0 * P::BPP, kbase + (size_t)px0 * P::BPP, npx, mw, kw);
-        uint32_t m[P::PPW], k[P::PPW];
-        P::unpack(mw, m);
-        P::unpack(kw, k);
-        hscan<DT, FWD>(m, k, carry, lane);
-        const uint32_t nw = P::pack(m);
-        if (npx > 0 && nw != mw) store_word_plain<DT>(mbase + (size_t)px0 * P::BPP, npx, nw);
-        carry = FWD ? __shfl_sync(FULL, m[P::PPW - 1], 31) : __shfl_sync(FULL, m[0], 0);
+    };
+    uint32_t mq[kXAhead], kq[kXAhead];
+#pragma unroll
+    for (int q = 0; q < kXAhead; ++q) fetch(q, mq[q], kq[q]);
+    uint32_t carry = P::MINPX;
+    for (int c0 = 0; c0 < chunks; c0 += kXAhead) {
+#pragma unroll
+        for (int q = 0; q < kXAhead; ++q) {
+            const int cc = c0 + q;
+            if (cc >= chunks) break;  // warp-uniform
+            const uint32_t mw = mq[q], kw = kq[q];
+            fetch(cc + kXAhead, mq[q], kq[q]);
+            uint32_t m[P::PPW], k[P::PPW];
+            P::unpack(mw, m);
+            P::unpack(kw, k);
+            hscan<DT, FWD>(m, k, carry, lane);
+            const uint32_t nw = P::pack(m);
+            const int px0 = px0_of(cc), npx = d.W - px0;
+            if (npx > 0 && nw != mw) store_word_plain<DT>(mbase + (size_t)px0 * P::BPP, npx, nw);
+            carry = FWD ? __shfl_sync(FULL, m[P::PPW - 1], 31) : __shfl_sync(FULL, m[0], 0);
+        }
     }
 }
 
