@@ -195,6 +195,30 @@ __device__ __forceinline__ long long globaltimer_ns() {
     return t;
 }
 
+// ------------------------------------------------ clamp-map scan steps
+// Carrying a value x through a run of pixels along the scan direction maps
+// it to max(min(x, B), A) (B: the run's least mask, A: the run's last pixel
+// without a carry).  One step of the warp's inclusive scan composes a lane's
+// map after the map of the lanes d before it:
+//   A = max(min(A_prev, B), A),  B = min(B_prev, B).
+// A lane with no source at distance d reads its own map back, and a clamp
+// map composed with itself is itself, so no lane predicate is needed.
+// uint8 / uint16: (A, B) share one word, A in the low half, and a step is
+// one shuffle, one 16x2 min and one 16x2 max on the critical path.
+template <bool FWD>
+__device__ __forceinline__ uint32_t map_step_packed(uint32_t cur, int d) {
+    const uint32_t prev = FWD ? __shfl_up_sync(FULL, cur, d) : __shfl_down_sync(FULL, cur, d);
+    return __vmaxu2(__vminu2(prev, __byte_perm(cur, 0u, 0x3232)), cur & 0xffffu);
+}
+// int32: A and B in two words, signed order.
+template <bool FWD>
+__device__ __forceinline__ void map_step_i32(uint32_t& A, uint32_t& B, int d) {
+    const int Ap = FWD ? __shfl_up_sync(FULL, (int)A, d) : __shfl_down_sync(FULL, (int)A, d);
+    const int Bp = FWD ? __shfl_up_sync(FULL, (int)B, d) : __shfl_down_sync(FULL, (int)B, d);
+    A = (uint32_t)max(min(Ap, (int)B), (int)A);
+    B = (uint32_t)min(Bp, (int)B);
+}
+
 // ---------------------------------------------------- horizontal warp scan
 // Propagates along one row in scan order (FWD: left to right) with `cin` the
 // marker value of the halo pixel entering the row at the first lane.  The
@@ -228,23 +252,14 @@ __device__ __forceinline__ void hscan(uint32_t (&m)[Px<DT>::PPW], const uint32_t
         A = P::mx(A, P::mn(cin, B));
         B = P::MINPX;  // the entry lane becomes a constant: nothing before it
     }
+    if (DT == DT_I32) {
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        uint32_t Ap, Bp;
-        if (DT == DT_I32) {
-            Ap = FWD ? __shfl_up_sync(FULL, A, d) : __shfl_down_sync(FULL, A, d);
-            Bp = FWD ? __shfl_up_sync(FULL, B, d) : __shfl_down_sync(FULL, B, d);
-        } else {
-            uint32_t pk = A | (B << 16);
-            pk = FWD ? __shfl_up_sync(FULL, pk, d) : __shfl_down_sync(FULL, pk, d);
-            Ap = pk & 0xffffu;
-            Bp = pk >> 16;
-        }
-        const bool valid = FWD ? (lane >= d) : (lane + d < 32);
-        if (valid) {
-            A = P::mx(P::mn(Ap, B), A);
-            B = P::mn(Bp, B);
-        }
+        for (int d = 1; d < 32; d <<= 1) map_step_i32<FWD>(A, B, d);
+    } else {
+        uint32_t cur = A | (B << 16);
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) cur = map_step_packed<FWD>(cur, d);
+        A = cur & 0xffffu;
     }
     uint32_t c = FWD ? __shfl_up_sync(FULL, A, 1) : __shfl_down_sync(FULL, A, 1);
     if (lane == edge_lane) c = cin;
@@ -275,20 +290,28 @@ __device__ __forceinline__ void sweep(WarpSmem<TH>& sm, int lane, unsigned long 
     constexpr int N = P::PPW;
     uint32_t prev[N];
     bool prev_valid = false, prev_changed = false;
+    // the row words of step i are read during step i - 1 (only step i
+    // writes its row), so their shared-memory latency overlaps a scan
+    uint32_t next_m = sm.tm[(DOWN ? 1 : TH) * 32 + lane], next_k = sm.tk[(DOWN ? 1 : TH) * 32 + lane];
 #pragma unroll 1
     for (int i = 0; i < TH; ++i) {
         const int r = DOWN ? 1 + i : TH - i;  // SMEM row
         const int rp = DOWN ? r - 1 : r + 1;  // SMEM row before it in sweep order
+        const uint32_t old = next_m, kw = next_k;
+        if (i + 1 < TH) {
+            const int rn = DOWN ? r + 1 : r - 1;
+            next_m = sm.tm[rn * 32 + lane];
+            next_k = sm.tk[rn * 32 + lane];
+        }
         if (!prev_changed && !((dil >> (r - 1)) & 1ull)) {
             prev_valid = false;
             continue;
         }
         if (!prev_valid) P::unpack(sm.tm[rp * 32 + lane], prev);
         ++row_steps;
-        const uint32_t old = sm.tm[r * 32 + lane];
         uint32_t m[N], k[N];
         P::unpack(old, m);
-        P::unpack(sm.tk[r * 32 + lane], k);
+        P::unpack(kw, k);
         if (CONN == 8) {
             uint32_t left = __shfl_up_sync(FULL, prev[N - 1], 1);
             uint32_t right = __shfl_down_sync(FULL, prev[0], 1);
@@ -442,26 +465,21 @@ __device__ __forceinline__ void hscan_rows(uint32_t (&m)[R][Px<DT>::PPW], const 
             B[q] = P::MINPX;  // the entry lane becomes a constant: nothing before it
         }
     }
+    if (DT == DT_I32) {
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const bool valid = FWD ? (lane >= d) : (lane + d < 32);
+        for (int d = 1; d < 32; d <<= 1)
 #pragma unroll
-        for (int q = 0; q < R; ++q) {
-            uint32_t Ap, Bp;
-            if (DT == DT_I32) {
-                Ap = FWD ? __shfl_up_sync(FULL, A[q], d) : __shfl_down_sync(FULL, A[q], d);
-                Bp = FWD ? __shfl_up_sync(FULL, B[q], d) : __shfl_down_sync(FULL, B[q], d);
-            } else {
-                uint32_t pk = A[q] | (B[q] << 16);
-                pk = FWD ? __shfl_up_sync(FULL, pk, d) : __shfl_down_sync(FULL, pk, d);
-                Ap = pk & 0xffffu;
-                Bp = pk >> 16;
-            }
-            if (valid) {
-                A[q] = P::mx(P::mn(Ap, B[q]), A[q]);
-                B[q] = P::mn(Bp, B[q]);
-            }
-        }
+            for (int q = 0; q < R; ++q) map_step_i32<FWD>(A[q], B[q], d);
+    } else {
+        uint32_t cur[R];
+#pragma unroll
+        for (int q = 0; q < R; ++q) cur[q] = A[q] | (B[q] << 16);
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1)
+#pragma unroll
+            for (int q = 0; q < R; ++q) cur[q] = map_step_packed<FWD>(cur[q], d);
+#pragma unroll
+        for (int q = 0; q < R; ++q) A[q] = cur[q] & 0xffffu;
     }
 #pragma unroll
     for (int q = 0; q < R; ++q) {
