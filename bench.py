@@ -104,6 +104,9 @@ class ClockSampler:
         self.thread = None
 
     def start(self):
+        """Starts sampling and returns once the first sample has arrived:
+        nvidia-smi's start-up takes driver locks that stall CUDA calls for
+        tens of milliseconds, which must not fall inside a timed region."""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -113,6 +116,10 @@ class ClockSampler:
             return
         self.thread = threading.Thread(target=self._read, daemon=True)
         self.thread.start()
+        t0 = time.perf_counter()
+        while not self.lines and self.proc.poll() is None and time.perf_counter() - t0 < 10.0:
+            time.sleep(0.01)
+        time.sleep(0.05)
 
     def _read(self):
         for line in self.proc.stdout:
