@@ -161,13 +161,13 @@ int resident_warps64(int variant, int device) {
 }
 
 // Tile height for calls that leave it at its default: 64-row tiles (fewer
-// tile boundaries to cross, fewer revisits) for jobs with at least four of
-// them per warp the grid keeps resident; below that the warps run short of
-// independent tiles whenever the front narrows, and 32-row tiles (twice the
-// tiles, twice the resident warps) finish sooner.  Measured on single
-// h-dome images from 2048^2 to 6144^2 u8 (up to 2.5 tiles per warp):
-// 32-row tiles 3-35 % faster; 64-image batches and one 16384^2 image
-// (18-20 tiles per warp): 64-row tiles 3-7 % faster.
+// tile boundaries to cross, fewer revisits) for jobs with at least two and a
+// half of them per warp the grid keeps resident; below that the warps run
+// short of independent tiles whenever the front narrows, and 32-row tiles
+// (twice the tiles) finish sooner.  Measured on single h-dome images:
+// 2048^2-4096^2 uint8 and 4096^2 uint16 (0.3-2.2 tiles per warp) 5-25 %
+// faster with 32 rows; 6144^2 and 8192^2 uint8 (2.5-4.5 per warp), the
+// 64-image batch and 16384^2 images (18-20 per warp) faster with 64.
 int default_tile_rows(int variant, long long tiles64) {
     int device = -1;
     if (cudaGetDevice(&device) != cudaSuccess) {
@@ -175,7 +175,7 @@ int default_tile_rows(int variant, long long tiles64) {
         return 64;
     }
     const int resident = resident_warps64(variant, device);
-    return resident > 0 && tiles64 < 4ll * resident ? 32 : 64;
+    return resident > 0 && 2ll * tiles64 < 5ll * resident ? 32 : 64;
 }
 
 long long job_tiles64(const iwpp_image* imgs, int n) {

@@ -86,7 +86,7 @@ def test_default_tile_height_follows_the_tile_count():
     iwpp.tune_clear()
     # 88 tiles of 64 rows: fewer than the device keeps warps resident
     assert iwpp.tile_count(1000, 700, 0, 0) == iwpp.tile_count(1000, 700, 0, 32)
-    # 65536 tiles of 64 rows: more than four per warp any device keeps resident
+    # 65536 tiles of 64 rows: more than 2.5 per warp any device keeps resident
     assert iwpp.tile_count(32768, 16384, 0, 0) == iwpp.tile_count(32768, 16384, 0, 64)
 
 
