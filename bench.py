@@ -684,7 +684,9 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "variant": variant, "tile_rows": args.tile_rows or "default",
+        "config": {"workload": WORKLOAD, "variant": variant,
+                   "tile_rows": args.tile_rows or ("default: %d" % (32 if iwpp.tile_count(W, H, 0, 0) ==
+                                                                      iwpp.tile_count(W, H, 0, 32) else 64)),
                    "l2": "inputs larger than L2: 6 working + 6 pristine markers + mask = 218 MB per step",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "bitexact": bitexact,
