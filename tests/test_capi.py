@@ -61,6 +61,16 @@ def test_tile_counts():
     assert lib.iwpp_tile_count(10, 10, 7, 64) == -1
 
 
+def test_default_tile_height_without_a_device():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("with a device the default follows its resident warps (tests/test_tune.py)")
+    lib = iwpp.load()
+    # no device to size the grid by: the default is 64 rows
+    assert lib.iwpp_tile_count(4096, 4096, 0, 0) == lib.iwpp_tile_count(4096, 4096, 0, 64)
+    assert lib.iwpp_tile_count(100, 100, 1, 0) == lib.iwpp_tile_count(100, 100, 1, 64)
+
+
 def test_workspace_bytes_grow_with_tiles():
     lib = iwpp.load()
     a = lib.iwpp_workspace_bytes(1000, 2, 0)
