@@ -57,7 +57,8 @@ typedef enum iwpp_queue_variant {
  * when it holds an entry for the job's workload class (iwpp_autotune). */
 typedef struct iwpp_config {
     int tile_rows;             /* 32 or 64 rows per tile; 0 = default: 64, or 32 when the
-                                  job has fewer than 2.5 64-row tiles per resident warp */
+                                  job has fewer than 2.5 64-row tiles per resident warp
+                                  (mutex queue: always 64) */
     long long queue_capacity;  /* entries per queue buffer; 0 = default; < 0: that multiple
                                   of the job's tile count */
     int init_passes;           /* whole-image passes first (+X, +Y, -X, -Y each); -1 = default (0) */

@@ -168,7 +168,11 @@ int resident_warps64(int variant, int device) {
 // 2048^2-4096^2 uint8 and 4096^2 uint16 (0.3-2.2 tiles per warp) 5-25 %
 // faster with 32 rows; 6144^2 and 8192^2 uint8 (2.5-4.5 per warp), the
 // 64-image batch and 16384^2 images (18-20 per warp) faster with 64.
+// The mutex queue is bound by its one lock (every take and insert is a
+// critical section), so its cost grows with the tile count: 64 rows always
+// (4096^2 uint8: 26 ms with 2048 tiles, 45 ms with 4096).
 int default_tile_rows(int variant, long long tiles64) {
+    if (variant == IWPP_QUEUE_MUTEX) return 64;
     int device = -1;
     if (cudaGetDevice(&device) != cudaSuccess) {
         cudaGetLastError();
