@@ -304,7 +304,8 @@ IWPP_API int iwpp_server_submit(iwpp_server s, const void *marker, const void *m
                                 int connectivity, unsigned long long *ticket);
 /* Waits up to timeout_ms (< 0: forever) for a ticket; IWPP_ERR_BUSY if it
  * is not finished by then.  On completion returns the request's status,
- * fills `result` (nullable) and forgets the ticket. */
+ * fills `result` (nullable) and forgets the ticket: one waiter gets the
+ * result, any other wait on the same ticket returns IWPP_ERR_INVALID. */
 IWPP_API int iwpp_server_wait(iwpp_server s, unsigned long long ticket, int timeout_ms, iwpp_request_result *result);
 IWPP_API int iwpp_server_stats_get(iwpp_server s, iwpp_server_stats *stats);
 /* Finishes every submitted request, then stops the lanes and frees the pool. */

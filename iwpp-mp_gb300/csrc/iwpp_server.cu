@@ -347,14 +347,21 @@ int iwpp_server_submit(iwpp_server s, const void* marker, const void* mask, void
 int iwpp_server_wait(iwpp_server s, unsigned long long ticket, int timeout_ms, iwpp_request_result* result) {
     if (!s) return IWPP_ERR_INVALID;
     std::unique_lock<std::mutex> lk(s->mu);
-    auto it = s->live.find(ticket);
-    if (it == s->live.end()) return IWPP_ERR_INVALID;
-    Request* r = it->second;
+    if (s->live.find(ticket) == s->live.end()) return IWPP_ERR_INVALID;
+    // Looked up again on every wake-up: another thread waiting on the same
+    // ticket may have taken the result (and freed the request) meanwhile.
+    auto ready = [&] {
+        auto f = s->live.find(ticket);
+        return f == s->live.end() || f->second->done;
+    };
     if (timeout_ms < 0) {
-        s->cv_done.wait(lk, [&] { return r->done; });
-    } else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return r->done; })) {
+        s->cv_done.wait(lk, ready);
+    } else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
         return IWPP_ERR_BUSY;
     }
+    auto it = s->live.find(ticket);
+    if (it == s->live.end()) return IWPP_ERR_INVALID;  // taken by another waiter
+    Request* r = it->second;
     if (result) {
         result->status = r->status;
         result->lane = r->lane;

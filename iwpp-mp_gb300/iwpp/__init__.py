@@ -542,9 +542,12 @@ class Server:
 
     def wait(self, ticket: int, timeout_ms: int = -1):
         r = RequestResult()
+        r.status = -1  # filled only by the wait that takes the ticket's result
         st = load().iwpp_server_wait(self._p, ticket, timeout_ms, ctypes.byref(r))
         if st == 7:
             raise TimeoutError(f"request {ticket} not finished")
+        if r.status == -1:  # unknown ticket, or another waiter took its result
+            raise IwppError(st, "iwpp_server_wait")
         held = self._held.pop(ticket, None)
         if st != 0:
             raise IwppError(st, "iwpp_server_wait")

@@ -134,3 +134,31 @@ def test_empty_request_completes():
     with iwpp.Server(lanes=1) as srv:
         out, info = srv.wait(srv.submit(a, a, 8))
         assert info["status"] == 0 and out.shape == (0, 5)
+
+
+def test_two_waiters_on_one_ticket():
+    # one waiter gets the result, the other IWPP_ERR_INVALID; neither reads
+    # a request the other has released
+    mask = synth.noise_mask(2048, 2048, 0, 21, 3.0, 5)
+    marker = synth.hdome_marker(mask, 60)
+    ref = oracle.reconstruct(marker, mask, 8)
+    lib = iwpp.load()
+    with iwpp.Server(lanes=1) as srv:
+        for _ in range(3):
+            out = np.zeros_like(mask)
+            t = srv.submit(marker, mask, 8, out=out)
+            statuses = []
+
+            def waiter():
+                r = iwpp.RequestResult()
+                statuses.append(lib.iwpp_server_wait(srv._p, t, -1, __import__("ctypes").byref(r)))
+
+            ths = [threading.Thread(target=waiter) for _ in range(2)]
+            for th in ths:
+                th.start()
+            for th in ths:
+                th.join()
+            assert sorted(statuses) == [0, 1]
+            assert np.array_equal(out, ref)
+            with pytest.raises(iwpp.IwppError):
+                srv.wait(t)  # forgotten
