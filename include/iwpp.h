@@ -53,8 +53,9 @@ typedef enum iwpp_queue_variant {
 } iwpp_queue_variant;
 
 /* Fields left at their defaults (tile_rows 0, queue_capacity 0,
- * init_passes -1, solver 0; or cfg NULL) are taken from the tuning table
- * when it holds an entry for the job's workload class (iwpp_autotune). */
+ * init_passes -1, solver 0, front_passes 0; or cfg NULL) are taken from the
+ * tuning table when it holds an entry for the job's workload class
+ * (iwpp_autotune). */
 typedef struct iwpp_config {
     int tile_rows;             /* 32 or 64 rows per tile; 0 = default: 64, or 32 when the
                                   job has fewer than 2.5 64-row tiles per resident warp
@@ -71,6 +72,17 @@ typedef struct iwpp_config {
     int solver;                /* in-tile solver: 0 = automatic, 1 = row sweeps (fewest
                                   instructions), 2 = vertical / horizontal passes
                                   (shortest latency) */
+    int front_passes;          /* whole-image directional passes restricted to the tiles that
+                                  changed since the last pass in the same direction, repeated
+                                  until no tile changes, then the tile engine on the tiles left
+                                  unsettled: 0 = default (the tuning table's choice, else the
+                                  tile engine alone), 1 = always, 2 = never */
+    int phantom_work;          /* fault-injection hook for tests, 0 normally.  1: the job counts
+                                  one unit of work that never arrives (a queue entry nobody
+                                  inserts; for the round-based queues a CTA that never reaches
+                                  the round barrier), so every device-side wait runs out and the
+                                  call returns IWPP_ERR_TIMEOUT after timeout_ms, the kernel
+                                  having returned */
 } iwpp_config;
 
 typedef struct iwpp_stats {
@@ -240,11 +252,13 @@ IWPP_API int iwpp_sweep_timing(void *marker, const void *mask, size_t pitch_mark
  * int32); larger images return IWPP_ERR_TOO_LARGE.  Uses the async queue,
  * 64-row tiles, plain loads; synchronous on `stream` (NULL = legacy default
  * stream).  The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  All calls share the one array: calls whose
- * work overlaps on the GPU (concurrent host threads or streams) race and
- * must be serialised by the caller.  Each call clears the state it needs;
- * the array otherwise keeps the last call's contents. */
+ * (cudaGetSymbolAddress) and the engine's launch shape with that device
+ * current; make that first call before any stream capture.  Both are kept
+ * until the process exits, so a cudaDeviceReset between calls is not
+ * supported (the kept address would be stale).  All calls share the one
+ * array: calls whose work overlaps on the GPU (concurrent host threads or
+ * streams) race and must be serialised by the caller.  Each call clears the
+ * state it needs; the array otherwise keeps the last call's contents. */
 #define IWPP_NOALLOC_SCRATCH_BYTES (4u << 20)
 IWPP_API int iwpp_reconstruct_noalloc(void *marker, const void *mask, size_t pitch_marker, size_t pitch_mask,
                                       int width, int height, int dtype, int connectivity, void *stream);
@@ -254,7 +268,9 @@ IWPP_API int iwpp_reconstruct_noalloc(void *marker, const void *mask, size_t pit
  * IWPP MP/src/main.cu:59).  Requests (host marker / mask / result buffers)
  * are submitted from any thread and admitted in arrival order while their
  * device bytes (staging copies of both planes plus queue state) fit the
- * memory budget.  `lanes` worker threads, each with its own stream and
+ * memory budget and the device's free memory at admission time (minus a
+ * headroom), so memory that other users of the device take or return after
+ * the server was created is seen by the next admission.  `lanes` worker threads, each with its own stream and
  * workspace, take every admitted request that is waiting when they come
  * free and run them as one batch (one persistent launch), so requests
  * arriving while others run join the next batch and their copies and
@@ -269,6 +285,11 @@ typedef struct iwpp_server_config {
     int lane_ctas;             /* CTAs per batch launch, 0 = the whole GPU */
     int timeout_ms;            /* device wait bound per batch, 0 = 60000 */
     long long memory_budget;   /* device bytes for admitted requests, 0 = half the free memory at creation */
+    long long memory_headroom; /* device bytes every admission leaves free for other users of
+                                  the device: a batch is admitted only while the device's free
+                                  memory at that moment (plus what the server's pool holds
+                                  unused) covers it and this headroom; 0 = 256 MiB, < 0 = no
+                                  live check (the budget alone) */
 } iwpp_server_config;
 
 typedef struct iwpp_request_result {
@@ -288,6 +309,8 @@ typedef struct iwpp_server_stats {
     long long bytes_in_use;    /* device bytes held by admitted requests now */
     long long bytes_peak;      /* most ever held at once */
     long long memory_budget;
+    long long held_back;       /* admissions deferred because the device's free memory at the
+                                  time (minus the headroom) could not hold the next request */
 } iwpp_server_stats;
 
 typedef struct iwpp_server_s *iwpp_server;

@@ -57,8 +57,10 @@ struct Config {
     int clip_marker;
     int plain_loads;
     int solver;
+    int front_passes;  // 0 default, 1 always, 2 never
+    int phantom_work;
     // fields the caller left at their defaults (the tuning table may fill them)
-    bool dflt_tile, dflt_queue, dflt_init, dflt_solver;
+    bool dflt_tile, dflt_queue, dflt_init, dflt_solver, dflt_front;
 };
 
 Config resolve_config(const iwpp_config* c) {
@@ -72,10 +74,13 @@ Config resolve_config(const iwpp_config* c) {
     r.clip_marker = c ? c->clip_marker : 0;
     r.plain_loads = c ? c->plain_loads : 0;
     r.solver = c && c->solver >= 0 && c->solver <= 2 ? c->solver : 0;
+    r.front_passes = c && c->front_passes >= 0 && c->front_passes <= 2 ? c->front_passes : 0;
+    r.phantom_work = c && c->phantom_work == 1 ? 1 : 0;
     r.dflt_tile = r.tile_rows == 0;
     r.dflt_queue = r.queue_capacity == 0;
     r.dflt_init = !c || c->init_passes < 0;
     r.dflt_solver = r.solver == 0;
+    r.dflt_front = r.front_passes == 0;
     if (std::getenv("IWPP_PLAIN_LOADS")) r.plain_loads = 1;
     return r;
 }
@@ -282,7 +287,8 @@ int build_job(Job& job, const iwpp_image* imgs, int n, int variant, const iwpp_c
               int staging, bool use_table = true) {
     job.cfg = resolve_config(cfgp);
     job.variant = resolve_variant(variant);
-    if (use_table && n > 0 && (job.cfg.dflt_tile || job.cfg.dflt_queue || job.cfg.dflt_init || job.cfg.dflt_solver)) {
+    if (use_table && n > 0 &&
+        (job.cfg.dflt_tile || job.cfg.dflt_queue || job.cfg.dflt_init || job.cfg.dflt_solver || job.cfg.dflt_front)) {
         // fields left at their defaults come from the tuning table, if it
         // has an entry for this workload class
         std::vector<int> dts, cns;
@@ -300,6 +306,7 @@ int build_job(Job& job, const iwpp_image* imgs, int n, int variant, const iwpp_c
             if (job.cfg.dflt_solver) job.cfg.solver = e.solver;
             if (job.cfg.dflt_init) job.cfg.init_passes = e.init_passes;
             if (job.cfg.dflt_queue && e.queue_mult > 0) job.cfg.queue_capacity = -(long long)e.queue_mult;
+            if (job.cfg.dflt_front) job.cfg.front_passes = e.front_passes ? 1 : 2;
         }
     }
     int th = job.cfg.tile_rows;
@@ -556,6 +563,7 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
     a.timeout_ns = (long long)job.cfg.timeout_ms * 1000000ll;
     a.max_restarts = job.cfg.max_restarts;
     a.solver = job.cfg.solver;
+    a.phantom = job.cfg.phantom_work;
 
     cudaError_t e = cudaSuccess;
     if (upload_descs && !job.descs.empty()) {
@@ -1188,7 +1196,7 @@ int iwpp_autotune(iwpp_handle h, const iwpp_image* images, int n, int variant, i
         }
         if (!dts.empty()) {
             TuneEntry e{best.tile_rows, best.solver, best.init_passes,
-                        best.queue_capacity < 0 ? (int)-best.queue_capacity : 0};
+                        best.queue_capacity < 0 ? (int)-best.queue_capacity : 0, best.front_passes == 1 ? 1 : 0};
             tune_store(tune_key(v, dts.data(), cns.data(), pxs.data(), (int)dts.size()), e);
         }
         // leave the images reconstructed (with the winner)

@@ -520,7 +520,9 @@ __device__ bool grid_barrier_round(const EngineArgs& a) {
         const unsigned gen = ld_volatile(&c->bar_gen);
         __threadfence();
         const unsigned arrived = atomicAdd(&c->bar_count, 1u);
-        if (arrived == gridDim.x - 1u) {
+        // (with the phantom-work test hook the barrier waits for one CTA
+        // more than the grid has, so every waiter runs out of time)
+        if (arrived == gridDim.x - 1u + (a.phantom ? 1u : 0u)) {
             // Round transition (IWPP MP DQ/src/globalQueue.cu:139-157 swapQueues,
             // UQ/src/globalQueue.cu:159-168 resetReadQueue, and the overflow
             // restart of DQ/MR.cu:1242-1323, all on the device).
@@ -668,6 +670,10 @@ __global__ void engine_init_kernel(EngineArgs a, int variant) {
         c->ahead = 0u;
         c->atail = a.G;
         if (variant == VAR_ASYNC) c->pending = (int)a.G;
+        // test hook: one pending entry that nobody inserts or finishes, so
+        // the waiting warps never see the job end and their bounded waits
+        // run out (the round-based queues stall at their barrier instead)
+        if (a.phantom) c->pending += 1;
         c->visits = 0ull;
         c->sweeps = 0ull;
         c->pushes = 0ull;

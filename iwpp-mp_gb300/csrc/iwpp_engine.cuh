@@ -79,6 +79,7 @@ struct EngineArgs {
     long long timeout_ns;
     int max_restarts;
     int solver;  // 0 automatic, 1 row sweeps, 2 passes
+    int phantom;  // test hook: one unit of work that never arrives (every wait runs out)
 };
 
 }  // namespace iwpp

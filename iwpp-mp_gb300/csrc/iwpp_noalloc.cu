@@ -15,6 +15,8 @@
 // exits.  In host code the array's name is only a host-side stand-in, not a
 // device address, so the device address is obtained once per device with
 // cudaGetSymbolAddress (with that device current) and passed to the kernels.
+// That address is kept for the life of the process: a cudaDeviceReset
+// between calls (which reloads the module) is not supported.
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -27,26 +29,42 @@ namespace {
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[IWPP_NOALLOC_SCRATCH_BYTES];
 
+// The counters and the one image descriptor each take one 256-byte slot at
+// the start of the scratch (the size bound below counts on it).
+static_assert(sizeof(Ctrl) <= 256 && sizeof(ImgDesc) <= 256, "scratch header slots");
+
 constexpr int kMaxDevices = 64;
 constexpr int kNoallocTileRows = 64;
 
 std::mutex g_setup_mu;
 unsigned char* g_scratch_ptr[kMaxDevices] = {};
+LaunchInfo g_launch[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device (set up on the
-// first call per device).
-int scratch_address(int device, unsigned char** out) {
+// Per-device set-up, done by the first call on a device with that device
+// current: the device address of the scratch array and the engine's launch
+// shape (kernel attributes, occupancy, SM count), both kept for the life of
+// the process so that later calls do no host-side queries.  A
+// cudaDeviceReset between calls would leave both stale; it is not supported.
+int device_setup(int device, unsigned char** out, LaunchInfo* li) {
     std::lock_guard<std::mutex> lk(g_setup_mu);
     if (!g_scratch_ptr[device]) {
         void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || p == nullptr) {
             cudaGetLastError();
             return IWPP_ERR_CUDA;
         }
+        LaunchInfo l{};
+        e = engine_prepare(VAR_ASYNC, kNoallocTileRows, device, &l);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return IWPP_ERR_CUDA;
+        }
+        g_launch[device] = l;
         g_scratch_ptr[device] = static_cast<unsigned char*>(p);
     }
     *out = g_scratch_ptr[device];
+    *li = g_launch[device];
     return IWPP_OK;
 }
 
@@ -94,7 +112,8 @@ extern "C" int iwpp_reconstruct_noalloc(void* marker, const void* mask, size_t p
         return IWPP_ERR_NO_DEVICE;
     }
     unsigned char* base = nullptr;
-    int rc = scratch_address(device, &base);
+    LaunchInfo li;
+    int rc = device_setup(device, &base, &li);
     if (rc != IWPP_OK) return rc;
 
     ImgDesc d{};
@@ -126,12 +145,8 @@ extern "C" int iwpp_reconstruct_noalloc(void* marker, const void* mask, size_t p
     a.solver = 0;
 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    LaunchInfo li;
-    cudaError_t e = engine_prepare(VAR_ASYNC, kNoallocTileRows, device, &li);
-    if (e == cudaSuccess) {
-        noalloc_store_desc<<<1, 1, 0, s>>>(reinterpret_cast<ImgDesc*>(base + off_img), d);
-        e = cudaGetLastError();
-    }
+    noalloc_store_desc<<<1, 1, 0, s>>>(reinterpret_cast<ImgDesc*>(base + off_img), d);
+    cudaError_t e = cudaGetLastError();
     // the init kernel clears the state words, the ring and the counters that
     // the previous call left in the scratch
     if (e == cudaSuccess) e = engine_launch_init(a, VAR_ASYNC, s);

@@ -67,6 +67,7 @@ struct iwpp_server_s {
     int tile_rows = 0;
     iwpp_config cfg{};
     long long budget = 0;
+    long long headroom = 0;  // < 0: no live check
     cudaMemPool_t pool = nullptr;
 
     std::mutex mu;
@@ -76,6 +77,7 @@ struct iwpp_server_s {
     std::unordered_map<unsigned long long, Request*> live;
     unsigned long long next_id = 1;
     long long in_use = 0;
+    long long unallocated = 0;  // admitted bytes whose pool allocations are not made yet
     bool stopping = false;
     iwpp_server_stats stats{};
 
@@ -88,6 +90,7 @@ struct iwpp_server_s {
 
     void lane_main(int li);
     int run_batch(Lane& lane, std::vector<Request*>& batch);
+    long long live_room();
 };
 
 namespace {
@@ -104,11 +107,32 @@ size_t request_bytes(int w, int h, int dtype, int tile_rows, size_t* pitch_out) 
 
 }  // namespace
 
+// Device bytes that admission may still hand out right now: the device's
+// free memory plus what the pool holds without using it, less the bytes
+// already admitted but not yet taken from the pool and the headroom left for
+// other users of the device.  Called with `mu` held.
+long long iwpp_server_s::live_room() {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    unsigned long long reserved = 0, used = 0;
+    if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) != cudaSuccess ||
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) != cudaSuccess) {
+        cudaGetLastError();
+        reserved = used = 0;
+    }
+    const long long idle = reserved > used ? (long long)(reserved - used) : 0ll;
+    return (long long)free_b + idle - unallocated - headroom;
+}
+
 int iwpp_server_s::run_batch(Lane& lane, std::vector<Request*>& batch) {
     cudaStream_t s = lane.stream;
     std::vector<iwpp_image> imgs;
     imgs.reserve(batch.size());
     cudaError_t e = cudaSuccess;
+    long long taken = 0;
     for (Request* r : batch) {
         if (r->w == 0 || r->h == 0) continue;
         const size_t row = (size_t)r->w * bpp_of(r->dtype);
@@ -120,6 +144,12 @@ int iwpp_server_s::run_batch(Lane& lane, std::vector<Request*>& batch) {
         if (e == cudaSuccess)
             e = cudaMemcpy2DAsync(r->d_mask, r->pitch, r->mask, r->pk, row, r->h, cudaMemcpyHostToDevice, s);
         imgs.push_back(iwpp_image{r->d_marker, r->d_mask, r->pitch, r->pitch, r->w, r->h, r->dtype, r->conn});
+        taken += (long long)r->bytes;
+    }
+    if (headroom >= 0) {
+        // the batch's planes are now the pool's (used) memory
+        std::lock_guard<std::mutex> lk(mu);
+        unallocated -= taken;
     }
     int rc = IWPP_OK;
     if (e != cudaSuccess) rc = e == cudaErrorMemoryAllocation ? IWPP_ERR_OOM : IWPP_ERR_CUDA;
@@ -155,17 +185,37 @@ void iwpp_server_s::lane_main(int li) {
         batch.clear();
         {
             std::unique_lock<std::mutex> lk(mu);
-            cv_work.wait(lk, [&] {
-                if (pending.empty()) return stopping;
-                return in_use + (long long)pending.front()->bytes <= budget;
-            });
-            if (pending.empty()) return;  // stopping and drained
+            // Admission: in arrival order while the budget holds and (live
+            // check) the device's free memory right now covers the batch
+            // plus the headroom.  Memory that another user of the device
+            // takes or gives back is seen here; since nothing signals it,
+            // a request held back by it is looked at again every millisecond.
+            long long room = 0;
+            for (;;) {
+                cv_work.wait(lk, [&] {
+                    if (pending.empty()) return stopping;
+                    return in_use + (long long)pending.front()->bytes <= budget;
+                });
+                if (pending.empty()) return;  // stopping and drained
+                // a server being destroyed finishes what is left regardless
+                // (a request the device cannot hold ends in IWPP_ERR_OOM)
+                if (headroom < 0 || stopping) break;
+                room = live_room();
+                if ((long long)pending.front()->bytes <= room) break;
+                stats.held_back += 1;
+                cv_work.wait_for(lk, std::chrono::milliseconds(1));
+            }
             const Clock::time_point now = Clock::now();
             while (!pending.empty() && (int)batch.size() < max_batch &&
-                   in_use + (long long)pending.front()->bytes <= budget) {
+                   in_use + (long long)pending.front()->bytes <= budget &&
+                   (headroom < 0 || stopping || (long long)pending.front()->bytes <= room)) {
                 Request* r = pending.front();
                 pending.pop_front();
                 in_use += (long long)r->bytes;
+                if (headroom >= 0) {
+                    room -= (long long)r->bytes;
+                    unallocated += (long long)r->bytes;
+                }
                 r->t_admit = now;
                 r->lane = li;
                 batch.push_back(r);
@@ -234,6 +284,7 @@ int iwpp_server_create(iwpp_server* out, int device, const iwpp_server_config* c
     size_t free_b = 0, total_b = 0;
     cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
     s->budget = c.memory_budget ? c.memory_budget : (long long)(free_b / 2);
+    s->headroom = c.memory_headroom ? (c.memory_headroom < 0 ? -1ll : c.memory_headroom) : (256ll << 20);
     s->stats.memory_budget = s->budget;
     cudaMemPoolProps props;
     std::memset(&props, 0, sizeof(props));

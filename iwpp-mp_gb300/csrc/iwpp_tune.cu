@@ -57,7 +57,8 @@ using namespace iwpp;
 namespace {
 bool valid_entry(const TuneEntry& e) {
     return (e.tile_rows == 32 || e.tile_rows == 64) && e.solver >= 0 && e.solver <= 2 && e.init_passes >= 0 &&
-           e.init_passes <= 64 && e.queue_mult >= 0 && e.queue_mult <= 1024;
+           e.init_passes <= 64 && e.queue_mult >= 0 && e.queue_mult <= 1024 && e.front_passes >= 0 &&
+           e.front_passes <= 1;
 }
 }  // namespace
 
@@ -68,12 +69,14 @@ int iwpp_tune_save(const char* path) {
     FILE* f = std::fopen(path, "w");
     if (!f) return IWPP_ERR_INVALID;
     std::lock_guard<std::mutex> lk(g_mu);
-    std::fprintf(f, "# iwpp tuning table v1: variant dtype conn pxclass batch tile_rows solver init_passes queue_mult\n");
+    std::fprintf(f,
+                 "# iwpp tuning table v2: variant dtype conn pxclass batch tile_rows solver init_passes queue_mult "
+                 "front_passes\n");
     for (const auto& kv : table()) {
         const TuneKey& k = kv.first;
         const TuneEntry& e = kv.second;
-        std::fprintf(f, "%d %d %d %d %d %d %d %d %d\n", k.variant, k.dtype, k.conn, k.pxclass, k.batch, e.tile_rows,
-                     e.solver, e.init_passes, e.queue_mult);
+        std::fprintf(f, "%d %d %d %d %d %d %d %d %d %d\n", k.variant, k.dtype, k.conn, k.pxclass, k.batch,
+                     e.tile_rows, e.solver, e.init_passes, e.queue_mult, e.front_passes);
     }
     const bool ok = std::fclose(f) == 0;
     return ok ? IWPP_OK : IWPP_ERR_INVALID;
@@ -89,10 +92,14 @@ int iwpp_tune_load(const char* path) {
     while (std::fgets(line, sizeof(line), f)) {
         if (line[0] == '#' || line[0] == '\n') continue;
         TuneKey k;
-        TuneEntry e;
-        if (std::sscanf(line, "%d %d %d %d %d %d %d %d %d", &k.variant, &k.dtype, &k.conn, &k.pxclass, &k.batch,
-                        &e.tile_rows, &e.solver, &e.init_passes, &e.queue_mult) != 9 ||
-            !valid_entry(e)) {
+        TuneEntry e{};
+        // v1 lines have nine fields (no front_passes: 0), v2 lines ten
+        char extra = 0;
+        const int got = std::sscanf(line, "%d %d %d %d %d %d %d %d %d %d %c", &k.variant, &k.dtype, &k.conn,
+                                    &k.pxclass, &k.batch, &e.tile_rows, &e.solver, &e.init_passes, &e.queue_mult,
+                                    &e.front_passes, &extra);
+        if (got == 9) e.front_passes = 0;
+        if ((got != 9 && got != 10) || !valid_entry(e)) {
             rc = IWPP_ERR_INVALID;
             break;
         }
@@ -130,6 +137,7 @@ int iwpp_tune_lookup(int variant, int dtype, int connectivity, long long pixels,
     out->solver = e.solver;
     out->init_passes = e.init_passes;
     out->queue_capacity = -e.queue_mult;  // negative: a multiple of the job's tile count
+    out->front_passes = e.front_passes ? 1 : 2;
     return IWPP_OK;
 }
 

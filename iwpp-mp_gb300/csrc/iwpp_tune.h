@@ -24,6 +24,7 @@ struct TuneEntry {
     int solver;      // 0 / 1 / 2
     int init_passes;
     int queue_mult;  // queue capacity in tiles per tile of the job; 0 = the variant's default
+    int front_passes;  // 0 = no front passes, 1 = front passes before the engine
 };
 
 int resolve_queue_variant(int variant);  // iwpp_api.cu: IWPP_QUEUE_DEFAULT -> the variant used

@@ -42,13 +42,13 @@ class Config(ctypes.Structure):
     _fields_ = [("tile_rows", ctypes.c_int), ("queue_capacity", ctypes.c_longlong),
                 ("init_passes", ctypes.c_int), ("grid_ctas", ctypes.c_int), ("max_restarts", ctypes.c_int),
                 ("timeout_ms", ctypes.c_int), ("clip_marker", ctypes.c_int), ("plain_loads", ctypes.c_int),
-                ("solver", ctypes.c_int)]
+                ("solver", ctypes.c_int), ("front_passes", ctypes.c_int), ("phantom_work", ctypes.c_int)]
 
     @classmethod
     def make(cls, tile_rows=0, queue_capacity=0, init_passes=-1, grid_ctas=0, max_restarts=0, timeout_ms=0,
-             clip_marker=0, plain_loads=0, solver=0):
+             clip_marker=0, plain_loads=0, solver=0, front_passes=0, phantom_work=0):
         return cls(tile_rows, queue_capacity, init_passes, grid_ctas, max_restarts, timeout_ms, clip_marker,
-                   plain_loads, solver)
+                   plain_loads, solver, front_passes, phantom_work)
 
 
 class Stats(ctypes.Structure):
@@ -74,7 +74,8 @@ class Image(ctypes.Structure):
 class ServerConfig(ctypes.Structure):
     _fields_ = [("lanes", ctypes.c_int), ("max_batch", ctypes.c_int), ("max_pending", ctypes.c_int),
                 ("variant", ctypes.c_int), ("tile_rows", ctypes.c_int), ("lane_ctas", ctypes.c_int),
-                ("timeout_ms", ctypes.c_int), ("memory_budget", ctypes.c_longlong)]
+                ("timeout_ms", ctypes.c_int), ("memory_budget", ctypes.c_longlong),
+                ("memory_headroom", ctypes.c_longlong)]
 
 
 class RequestResult(ctypes.Structure):
@@ -89,7 +90,7 @@ class RequestResult(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_longlong) for k in ("submitted", "completed", "failed", "rejected", "batches",
                                                  "largest_batch", "pixels", "bytes_in_use", "bytes_peak",
-                                                 "memory_budget")]
+                                                 "memory_budget", "held_back")]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -361,8 +362,8 @@ def autotune(pairs: Sequence, variant="default", repeats: int = 0, handle: Optio
         raise IwppError(st, "iwpp_autotune")
     b = res.best
     return {"tile_rows": b.tile_rows, "solver": b.solver, "init_passes": b.init_passes,
-            "queue_capacity": b.queue_capacity, "best_ms": res.best_ms, "default_ms": res.default_ms,
-            "candidates": res.candidates}
+            "front_passes": b.front_passes, "queue_capacity": b.queue_capacity, "best_ms": res.best_ms,
+            "default_ms": res.default_ms, "candidates": res.candidates}
 
 
 def fixed_point_violations(result, mask, connectivity: int = 8, stream=None) -> int:
@@ -412,7 +413,7 @@ def tune_lookup(variant, dtype: int, connectivity: int, pixels: int, batch: bool
     if st != 0:
         return None
     return {"tile_rows": c.tile_rows, "solver": c.solver, "init_passes": c.init_passes,
-            "queue_capacity": c.queue_capacity}
+            "front_passes": c.front_passes, "queue_capacity": c.queue_capacity}
 
 
 class Plan:
@@ -504,10 +505,10 @@ class Server:
 
     def __init__(self, device: int = 0, lanes: int = 0, max_batch: int = 0, max_pending: int = 0,
                  variant="default", tile_rows: int = 0, lane_ctas: int = 0, timeout_ms: int = 0,
-                 memory_budget: int = 0):
+                 memory_budget: int = 0, memory_headroom: int = 0):
         lib = load()
         cfg = ServerConfig(lanes, max_batch, max_pending, _variant(variant), tile_rows, lane_ctas, timeout_ms,
-                           memory_budget)
+                           memory_budget, memory_headroom)
         p = ctypes.c_void_p()
         st = lib.iwpp_server_create(ctypes.byref(p), device, ctypes.byref(cfg))
         if st != 0:

@@ -34,7 +34,9 @@ import numpy as np
 
 ORACLE_DIR = os.path.dirname(os.path.abspath(__file__))
 REF_OUT = os.path.join(ORACLE_DIR, "_ref")
-REFERENCE = "/root/reference"
+# where the reference checkout lies: IWPP_REFERENCE_DIR, else the recipe's
+# default location
+REFERENCE = os.environ.get("IWPP_REFERENCE_DIR", "/root/reference")
 VARIANT_DIRS = {"dq": "IWPP MP DQ", "uq": "IWPP MP UQ"}
 HARNESS_SRC = os.path.join(ORACLE_DIR, "refrun_harness.cpp")
 HARNESS_BIN = os.path.join(REF_OUT, "refrun_harness")

@@ -94,6 +94,41 @@ def test_admission_stays_within_the_memory_budget(reqs_and_refs):
         assert np.array_equal(out, refs[i // 2]), i
 
 
+def test_admission_sees_device_memory_taken_after_creation():
+    # Admission checks the device's free memory when a request comes up, not
+    # only the budget fixed at creation: memory another user of the device
+    # takes after the server started holds requests back until it is given
+    # back.
+    import torch
+    mask = synth.noise_mask(4096, 4096, 1, 31, 2.0, 3)   # uint16: a 64 MiB request
+    marker = synth.sparse_marker(mask, 32, 1e-4)
+    ref = oracle.reconstruct(marker, mask, 8)
+    mib = 1 << 20
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    free0, _ = torch.cuda.mem_get_info()
+    # after creation the server's pool holds its 256 MiB budget unused, so the
+    # room it sees is the free memory before creation less this headroom:
+    # about 1 GiB
+    with iwpp.Server(lanes=1, memory_budget=256 * mib, memory_headroom=free0 - 1024 * mib) as srv:
+        out, info = srv.wait(srv.submit(marker, mask, 8))
+        assert info["status"] == 0 and np.array_equal(out, ref)
+        held0 = srv.stats()["held_back"]
+        # another tenant takes all but ~30 MiB of that room
+        block = torch.empty(1024 * mib - 32 * mib, dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()
+        t = srv.submit(marker, mask, 8)
+        with pytest.raises(TimeoutError):  # not finished: held back
+            srv.wait(t, timeout_ms=300)
+        assert srv.stats()["held_back"] > held0
+        # ... and gives it back: the request is admitted and served
+        del block
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        out, info = srv.wait(t, timeout_ms=60000)
+        assert info["status"] == 0 and np.array_equal(out, ref)
+
+
 def test_request_larger_than_the_budget_is_refused():
     mask = synth.noise_mask(2048, 2048, 0, 9, 2.0, 3)
     marker = synth.hdome_marker(mask, 30)

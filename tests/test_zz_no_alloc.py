@@ -63,6 +63,74 @@ def test_noalloc_matches_allocating_entry_point_on_two_calls():
             assert np.array_equal(_host(out, marker.dtype), _host(ref, marker.dtype)), (call, dt, conn, w, h)
 
 
+def test_noalloc_allocates_nothing_and_runs_on_a_side_stream():
+    # A warm call (the device set-up is done) must leave the device's free
+    # memory as it was: no cudaMalloc, no pool growth, no library workspace.
+    # It runs on a non-default stream the caller owns.
+    import torch
+    lib = iwpp.load()
+    dt, conn, w, h = CASES[0]
+    mask = synth.noise_mask(w, h, dt, 977, 3.0, 8)
+    marker = synth.hdome_marker(mask, 35)
+    k = _dev(mask)
+    ref = _dev(marker)
+    assert lib.iwpp_reconstruct(None, ref.data_ptr(), k.data_ptr(), _pitch(ref), _pitch(k), w, h, dt, conn,
+                                iwpp.DEFAULT, None, None, None) == 0
+    outs = [_dev(marker) for _ in range(2)]
+    side = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    rc = lib.iwpp_reconstruct_noalloc(outs[0].data_ptr(), k.data_ptr(), _pitch(outs[0]), _pitch(k), w, h, dt, conn,
+                                      ctypes.c_void_p(side.cuda_stream))
+    assert rc == 0, iwpp.status_string(rc)
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    rc = lib.iwpp_reconstruct_noalloc(outs[1].data_ptr(), k.data_ptr(), _pitch(outs[1]), _pitch(k), w, h, dt, conn,
+                                      ctypes.c_void_p(side.cuda_stream))
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert rc == 0, iwpp.status_string(rc)
+    assert free_after >= free_before, free_before - free_after
+    for o in outs:
+        assert np.array_equal(_host(o, marker.dtype), _host(ref, marker.dtype))
+
+
+# Scratch layout of one call (iwpp_noalloc.cu): counters and the image
+# descriptor in the first 512 bytes, one state word per tile, then a ring of
+# two entries per tile, each part 256-byte aligned -- at most 767 + 12 bytes
+# per tile, at least 512 + 12.
+_SCRATCH = 4 << 20
+_TILES_FIT = (_SCRATCH - 767) // 12      # certainly fits
+_TILES_OVER = (_SCRATCH - 512) // 12 + 1  # certainly does not
+
+
+def test_noalloc_largest_image_that_fits_and_one_tile_row_more_than_that():
+    # A 4-pixel-wide uint8 image has one 128 x 64 tile per 64 rows, so the
+    # tile count sits right at the scratch bound with little memory (89 MB
+    # per plane).  Content is generated on the device: random noise and an
+    # h-dome marker (h = 40).
+    import torch
+    lib = iwpp.load()
+    w = 4
+    h = 64 * _TILES_FIT
+    g = torch.Generator(device="cuda")
+    g.manual_seed(1234)
+    mask = torch.randint(0, 256, (h, w), dtype=torch.uint8, device="cuda", generator=g)
+    marker = (mask.to(torch.int16) - 40).clamp_(min=0).to(torch.uint8)
+    ref = marker.clone()
+    out = marker.clone()
+    assert lib.iwpp_reconstruct(None, ref.data_ptr(), mask.data_ptr(), w, w, w, h, 0, 8, iwpp.DEFAULT, None, None,
+                                None) == 0
+    torch.cuda.synchronize()
+    rc = lib.iwpp_reconstruct_noalloc(out.data_ptr(), mask.data_ptr(), w, w, w, h, 0, 8, None)
+    assert rc == 0, iwpp.status_string(rc)
+    assert torch.equal(out, ref)
+    assert not torch.equal(out, marker)
+    # the same width with enough rows to pass the bound is refused before the
+    # (never dereferenced) pointers are touched
+    rc = lib.iwpp_reconstruct_noalloc(256, 256, w, w, w, 64 * _TILES_OVER, 0, 8, None)
+    assert rc == 8, iwpp.status_string(rc)
+
+
 def test_noalloc_refuses_rows_that_need_a_staging_copy():
     lib = iwpp.load()
     # a 513-byte pitch does not keep rows 4-byte aligned; the allocating entry
