@@ -1,41 +1,48 @@
 #!/usr/bin/env python3
 """Benchmark: Gpixels/s of bit-exact reconstruction by dilation on GB300.
 
-Workload (one "step"): the six plain 4096x4096 uint8 reconstructions of the
-4096^2 configuration -- connectivity {4, 8} x h-dome h {10, 40, 100} on one
-seeded smoothed-noise-plus-discs mask -- each through the C ABI with the
-async queue (--variant picks mutex / double / unique).  Every
-reconstruction restores its marker from a pristine device copy first (in
-place).
+Headline workload (one "step"): the plain 16384 x 16384 uint8 8-connected
+reconstruction of the spiral-corridor image -- smoothed noise (seed 2,
+sigma 16) with a one-pixel square spiral corridor at 255 (arm pitch 256,
+1 048 194 pixels) and a marker that is 0 except 64 seeds, one at the
+spiral's start -- the largest configuration that fits one GPU, through the
+C ABI (async queue by default; --variant picks mutex / double / unique).
+The library's autotuner is run once on the image class before the timed
+region (as a user would, once per class); every step then restores the
+marker from a pristine device copy and reconstructs with the default
+configuration fields, which the tuning table fills.
 
   value : device-resident throughput (inputs already in HBM), CUDA events
           around K steps on the launching stream, max over ranks.
-  e2e   : the same six reconstructions from pinned HOST buffers, H2D of
-          marker + mask and D2H of the result inside the timed region, each
-          image through the per-image C-ABI call with its copies on separate
-          streams (double-buffered, copies overlap the neighbouring images'
-          reconstructions); e2e.sync_call gives the same through the
-          synchronous call with copies and reconstruction back to back.
-  roofline : the persistent engine kernel; algorithmic bytes = 3 * W * H *
-          bytes/pixel per reconstruction (read mask, read marker, write
-          result) over the kernel's event-timed duration, against the
-          measured HBM copy bandwidth.
+  e2e   : the same reconstruction from pinned HOST buffers through the
+          per-image C-ABI call: H2D of marker + mask and D2H of the result
+          inside the timed region, copies on their own streams and
+          double-buffered so that one step's copies overlap its neighbours'
+          reconstructions.
+  roofline : one reconstruction (front passes + check + tile engine, all of
+          this library's kernels of the call) as the unit: algorithmic bytes
+          = 3 * W * H * bytes/pixel (read mask, read marker, write result)
+          over its CUDA-event duration, against the measured HBM copy
+          bandwidth.
   cpu_baseline : the CPU oracle (Vincent 1993 hybrid, single thread) on the
-          same six images, also used to check the GPU output bit for bit.
+          same image, which also checks the GPU output bit for bit.
 
 Sub-results in the same line (skipped with --no-extras):
+  config1 : the six 4096^2 uint8 reconstructions (connectivity {4, 8} x
+          h-dome h {10, 40, 100}), device-resident and end to end.
   batched : 64 uneven images in one CUDA-graph plan vs 64 sequential plain
           calls, Gpixels/s of each, bit-exact against each other and the
           oracle.
   served : a 2000 req/s Poisson stream through the serving loop (open loop:
           p50 / p99 latency; closed loop: saturated Gpixels/s) vs plain
           per-request calls, with host buffers, every result bit-exact.
-  spiral : the 16384^2 spiral-corridor worst case in uint8 / uint16 / int32.
+  spiral_types : the 16384^2 spiral in uint16 and int32, each checked
+          against the oracle.
 
 --impl reference times the reference's CPU path for the same workload.  The
-reference has no CPU implementation, so that is the oracle port on every
-host core (one image per thread at a time, up to 8 steps' worth of images),
-on the same metric and config.
+reference has no CPU implementation, so that is the oracle port: one copy
+of the headline reconstruction per host core at once, on the same metric
+and config.
 
 Multi-GPU (torchrun, N > 1): replicas only -- every rank reconstructs its own
 copy of the workload, no collective on the data path; value = all ranks'
@@ -60,8 +67,10 @@ for p in (os.path.join(REPO, "iwpp-mp_gb300"), REPO):
 
 METRIC = "Gpixels/s bit-exact reconstruction (plain vs batched); served p50/p99 latency"
 UNIT = "Gpixels/s"
-WORKLOAD = ("4096x4096 uint8 plain reconstruction, seed 1, sigma 8, 2000 discs, h-dome h in {10,40,100} x "
-            "connectivity {4,8} (6 images per step)")
+WORKLOAD = ("16384x16384 uint8 8-connected spiral-corridor reconstruction: smoothed noise (seed 2, sigma 16), "
+            "1-px square spiral corridor at 255 (arm pitch 256), marker 0 but 64 seeds (one per step)")
+CONFIG1 = ("4096x4096 uint8 plain reconstruction, seed 1, sigma 8, 2000 discs, h-dome h in {10,40,100} x "
+           "connectivity {4,8} (6 images per step)")
 
 
 def _dist_env():
@@ -155,7 +164,14 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-def load_workload():
+def load_headline():
+    """(marker, mask, corridor pixels) of the headline image."""
+    from iwpp import synth
+
+    return synth.config2(synth.U8)
+
+
+def load_config1():
     from iwpp import synth
 
     mask = synth.config1_mask()
@@ -165,27 +181,22 @@ def load_workload():
     return mask, cases
 
 
-def cpu_oracle_cases(mask, cases, threads: int):
-    """Runs the oracle on every case; returns (results, seconds)."""
+def timed_oracle(marker, mask, conn):
+    """(result, seconds) of one oracle reconstruction (one host thread)."""
     import oracle
-    from concurrent.futures import ThreadPoolExecutor
 
     t0 = time.perf_counter()
-    if threads <= 1:
-        res = [oracle.reconstruct(m, mask, conn) for conn, _, m in cases]
-    else:
-        with ThreadPoolExecutor(max_workers=threads) as ex:  # ctypes releases the GIL
-            res = list(ex.map(lambda c: oracle.reconstruct(c[2], mask, c[0]), cases))
+    res = oracle.reconstruct(marker, mask, conn)
     return res, time.perf_counter() - t0
 
 
-def traffic_from_profile():
-    path = os.path.join(REPO, "profiles", "engine_traffic.json")
+def traffic_from_profile(key):
+    """DRAM bytes per launch recorded from an ncu capture (profiles/)."""
+    path = os.path.join(REPO, "profiles", "dram_traffic.json")
     try:
         with open(path) as f:
-            d = json.load(f)
-        return d.get("bytes_per_launch")
-    except (OSError, ValueError):
+            return json.load(f)[key]["bytes_per_launch"]
+    except (OSError, ValueError, KeyError, TypeError):
         return None
 
 
@@ -198,40 +209,32 @@ def peak_hbm():
 
 
 def run_reference(args):
+    """The reference has no CPU path (its only implementation is CUDA), so the
+    reference arm times the oracle port: one copy of the headline
+    reconstruction per host thread at once (the oracle is sequential), on
+    every host core, once -- about 20-40 s of CPU work."""
     world, rank, _ = _dist_env()
     if rank != 0:
         return 0
-    import oracle
     from concurrent.futures import ThreadPoolExecutor
 
-    mask, cases = load_workload()
-    px_step = sum(m.size for _, _, m in cases)
-    threads = os.cpu_count() or 1
-    # The images of all steps on every host core at once (the oracle is one
-    # thread per image), bounded to 8 steps' worth so that large step counts
-    # still finish in a few minutes; the rate is per pixel either way.
-    n_jobs = min(args.steps, 8) * len(cases)
-    jobs = [cases[j % len(cases)] for j in range(n_jobs)]
-
-    def one(c):
-        oracle.reconstruct(c[2], mask, c[0])
-
+    marker, mask, _ = load_headline()
+    px = marker.size
+    threads = min(os.cpu_count() or 1, 16)
     with ThreadPoolExecutor(max_workers=threads) as ex:  # ctypes releases the GIL
-        if args.warmup > 0:
-            list(ex.map(one, cases))
         t0 = time.perf_counter()
-        list(ex.map(one, jobs))
+        list(ex.map(lambda _: timed_oracle(marker, mask, 8), range(threads)))
         t_total = time.perf_counter() - t0
-    value = n_jobs * (px_step / len(cases)) / t_total / 1e9
+    value = threads * px / t_total / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": px_step / (value * 1e9) * 1e3, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": px / (value * 1e9) * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "config": {"workload": WORKLOAD, "l2": "n/a (host)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{n_jobs} of the step's 4096x4096 uint8 reconstructions ({min(args.steps, 8)} "
-                                   f"steps' worth) on {threads} host threads, one image per thread at a time "
-                                   "(the reference has no CPU path; this is the oracle restatement)"},
+                         "sample": f"{threads} concurrent reconstructions of the 16384x16384 uint8 spiral image, one "
+                                   "per host thread (the reference has no CPU path; this is the oracle "
+                                   "restatement, Vincent 1993 hybrid)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -444,62 +447,177 @@ def bench_served(args, dev, variant):
             "bitexact_vs_oracle": oracle_ok}
 
 
-def bench_spiral(args, dev, variant):
-    """16384 x 16384 spiral-corridor worst case (seed 2, sigma 16, arm pitch
-    256, 64 seeds), uint8 / uint16 / int32, 8-connectivity."""
+def bench_config1(args, dev, variant, handle):
+    """The six 4096^2 uint8 reconstructions of configuration 1 per step:
+    device-resident (events on the launching stream) and end to end from
+    pinned host buffers, each image through the per-image C-ABI call."""
     import numpy as np
     import torch
+
+    import iwpp
+
+    lib = iwpp.load()
+    mask_np, cases = load_config1()
+    H, W = mask_np.shape
+    px_step = W * H * len(cases)
+    vcode = iwpp._variant(variant)
+    mask = torch.from_numpy(mask_np).to(dev)
+    pristine = [torch.from_numpy(m).to(dev) for _, _, m in cases]
+    work = [p.clone() for p in pristine]
+    conns = [c for c, _, _ in cases]
+    stream = torch.cuda.Stream(dev)
+    steps = max(args.steps, 20)
+
+    def step(ev_pairs=None):
+        for i in range(len(cases)):
+            work[i].copy_(pristine[i], non_blocking=True)
+            if ev_pairs is not None:
+                ev_pairs[i][0].record(stream)
+            st = lib.iwpp_reconstruct_async(handle.ptr, work[i].data_ptr(), mask.data_ptr(), W, W, W, H, 0, conns[i],
+                                            vcode, None, stream.cuda_stream)
+            if st != 0:
+                raise iwpp.IwppError(st, "iwpp_reconstruct_async")
+            if ev_pairs is not None:
+                ev_pairs[i][1].record(stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            step()
+        stream.synchronize()
+        results = [w.cpu().numpy() for w in work]
+    bitexact = None
+    if not args.no_cpu:
+        import oracle
+        from concurrent.futures import ThreadPoolExecutor
+
+        with ThreadPoolExecutor(max_workers=len(cases)) as ex:
+            refs = list(ex.map(lambda c: oracle.reconstruct(c[2], mask_np, c[0]), cases))
+        bitexact = all(np.array_equal(a, b) for a, b in zip(results, refs))
+    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in cases]
+          for _ in range(steps)]
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        t0.record(stream)
+        for k in range(steps):
+            step(ev[k])
+        t1.record(stream)
+    torch.cuda.synchronize()
+    elapsed = t0.elapsed_time(t1)
+    recon_ms = [a.elapsed_time(b) for row in ev for (a, b) in row]
+    mean_ms = sum(recon_ms) / len(recon_ms)
+    peak = peak_hbm()[0]
+
+    # end to end: H2D / reconstruction / D2H on three streams, double-buffered
+    host_m = [torch.from_numpy(m).pin_memory() for _, _, m in cases]
+    host_k = torch.from_numpy(mask_np).pin_memory()
+    host_out = [torch.empty(h.shape, dtype=h.dtype, pin_memory=True) for h in host_m]
+    s_in, s_run, s_out = (torch.cuda.Stream(dev) for _ in range(3))
+    dmb = [torch.empty((H, W), dtype=torch.uint8, device=dev) for _ in range(2)]
+    dkb = [torch.empty((H, W), dtype=torch.uint8, device=dev) for _ in range(2)]
+    ev_in = [torch.cuda.Event() for _ in range(2)]
+    ev_run = [torch.cuda.Event() for _ in range(2)]
+    ev_out = [torch.cuda.Event() for _ in range(2)]
+    for e in ev_out:
+        e.record(s_out)
+
+    def pipelined_step(finish=True):
+        for i in range(len(cases)):
+            b = i & 1
+            with torch.cuda.stream(s_in):
+                s_in.wait_event(ev_out[b])
+                dmb[b].copy_(host_m[i], non_blocking=True)
+                dkb[b].copy_(host_k, non_blocking=True)
+                ev_in[b].record(s_in)
+            s_run.wait_event(ev_in[b])
+            st = lib.iwpp_reconstruct_async(handle.ptr, dmb[b].data_ptr(), dkb[b].data_ptr(), W, W, W, H, 0,
+                                            conns[i], vcode, None, s_run.cuda_stream)
+            if st != 0:
+                raise iwpp.IwppError(st, "iwpp_reconstruct_async")
+            ev_run[b].record(s_run)
+            with torch.cuda.stream(s_out):
+                s_out.wait_event(ev_run[b])
+                host_out[i].copy_(dmb[b], non_blocking=True)
+                ev_out[b].record(s_out)
+        if finish:
+            s_out.synchronize()
+            st = lib.iwpp_handle_sync(handle.ptr, None)
+            if st != 0:
+                raise iwpp.IwppError(st, "iwpp_handle_sync")
+
+    for _ in range(max(args.warmup, 3)):
+        pipelined_step()
+    e2e_steps = min(steps, 40)
+    torch.cuda.synchronize()
+    ts = time.perf_counter()
+    for k in range(e2e_steps):
+        pipelined_step(finish=k == e2e_steps - 1)
+    secs = time.perf_counter() - ts
+    e2e_ok = all(np.array_equal(host_out[i].numpy(), results[i]) for i in range(len(cases)))
+    return {"workload": CONFIG1, "variant": variant, "steps": steps, "gpx_s": px_step * steps / (elapsed / 1e3) / 1e9,
+            "ms_per_step": elapsed / steps, "mean_reconstruction_ms": mean_ms,
+            "hbm_frac": 3 * W * H / (mean_ms / 1e3) / 1e9 / peak, "bitexact_vs_oracle": bitexact,
+            "dram_bytes_per_reconstruction": traffic_from_profile("config1"),
+            "e2e": {"gpx_s": px_step * e2e_steps / secs / 1e9, "steps": e2e_steps, "bitexact": e2e_ok,
+                    "h2d_bytes_per_step": len(cases) * 2 * W * H, "d2h_bytes_per_step": len(cases) * W * H}}
+
+
+def bench_spiral_types(args, dev, variant, handle):
+    """The 16384^2 spiral in uint16 and int32 (8-connectivity): untuned
+    default, then autotuned; each result checked against the oracle, which
+    runs on host threads while the GPU works."""
+    import numpy as np
+    import torch
+    from concurrent.futures import ThreadPoolExecutor
 
     import iwpp
     from iwpp import synth
 
     res = {}
-    h = iwpp.Handle(dev.index or 0)
     peak = peak_hbm()[0]
-    for name, dt in (("u8", synth.U8), ("u16", synth.U16), ("i32", synth.I32)):
+    ex = ThreadPoolExecutor(max_workers=2)
+    pending = []
+    for name, dt in (("u16", synth.U16), ("i32", synth.I32)):
         marker, mask, _ = synth.config2(dt)
         H, W = mask.shape
         bpp = mask.dtype.itemsize
+        fut = None if args.no_cpu else ex.submit(timed_oracle, marker, mask, 8)
         m0, k = _to_dev(marker, dev), _to_dev(mask, dev)
         m = m0.clone()
-        # the untuned default first, then the autotuned configuration for
-        # this image class (tile rows, solver, initial whole-image passes)
-        st0 = iwpp.reconstruct(m, k, connectivity=8, variant=variant, handle=h)
+        st0 = iwpp.reconstruct(m, k, connectivity=8, variant=variant, handle=handle)
         m.copy_(m0)
-        tuned = iwpp.autotune([(m, k, 8)], variant=variant, repeats=1, handle=h)
+        tuned = iwpp.autotune([(m, k, 8)], variant=variant, repeats=1, handle=handle)
         times = []
         for rep in range(1 + args.spiral_reps):
             m.copy_(m0)
             torch.cuda.synchronize()
-            st = iwpp.reconstruct(m, k, connectivity=8, variant=variant, handle=h)
+            st = iwpp.reconstruct(m, k, connectivity=8, variant=variant, handle=handle)
             if rep:
                 times.append(st.device_ms)
         t = statistics.median(times) / 1e3
-        entry = {"ms": t * 1e3, "gpx_s": W * H / t / 1e9, "hbm_frac": 3 * W * H * bpp / t / 1e9 / peak,
-                 "visits": st.visits, "tiles": st.tiles, "untuned_ms": st0.device_ms,
-                 "autotuned": {k_: tuned[k_] for k_ in ("tile_rows", "solver", "init_passes")}}
-        if name == "u8" and not args.no_cpu:
-            import oracle
-
-            t0 = time.perf_counter()
-            ref = oracle.reconstruct(marker, mask, 8)
-            entry["cpu_oracle_s"] = time.perf_counter() - t0
-            entry["bitexact_vs_oracle"] = bool(np.array_equal(_from_dev(m, marker.dtype), ref))
-            del ref
-        res[name] = entry
+        res[name] = {"ms": t * 1e3, "gpx_s": W * H / t / 1e9, "hbm_frac": 3 * W * H * bpp / t / 1e9 / peak,
+                     "visits": st.visits, "tiles": st.tiles, "front_sweeps": st.front_sweeps,
+                     "untuned_ms": st0.device_ms,
+                     "autotuned": {k_: tuned[k_] for k_ in ("tile_rows", "solver", "init_passes", "front_passes")}}
+        pending.append((name, fut, _from_dev(m, marker.dtype)))
         del m, m0, k
         torch.cuda.empty_cache()
-    h.close()
+    for name, fut, out in pending:
+        if fut is not None:
+            ref, secs = fut.result()
+            res[name]["bitexact_vs_oracle"] = bool(np.array_equal(out, ref))
+            res[name]["cpu_oracle_s"] = secs
+    ex.shutdown()
     res["workload"] = ("16384x16384, 8-conn, smoothed noise (seed 2, sigma 16) with a 1-px spiral corridor "
-                       "(arm pitch 256) at the dtype maximum, marker 0 but 64 seeds; device time per "
-                       f"reconstruction with the autotuned configuration, median of {args.spiral_reps} "
-                       "(untuned_ms: the default configuration)")
+                       "(arm pitch 256) at the dtype maximum, marker the dtype minimum but 64 seeds; device time "
+                       f"per reconstruction with the autotuned configuration, median of {args.spiral_reps}")
     return res
 
 
 def run_ours(args):
     import numpy as np
     import torch
+    from concurrent.futures import ThreadPoolExecutor
 
     import iwpp
 
@@ -511,53 +629,55 @@ def run_ours(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     variant = args.variant
-    mask_np, cases = load_workload()
+    marker_np, mask_np, n_corridor = load_headline()
     H, W = mask_np.shape
-    px_step = W * H * len(cases)
+    px = W * H
     bytes_per_recon = 3 * W * H * 1
+    # the oracle (one host thread) runs while the GPU works: the CPU baseline
+    # and the bit-exact check of the headline result
+    oracle_ex = ThreadPoolExecutor(max_workers=1)
+    oracle_fut = None
+    if rank == 0 and not args.no_cpu:
+        oracle_fut = oracle_ex.submit(timed_oracle, marker_np, mask_np, 8)
 
-    # device-resident inputs: one mask, pristine markers, working markers
     mask = torch.from_numpy(mask_np).to(dev)
-    pristine = [torch.from_numpy(m).to(dev) for _, _, m in cases]
-    work = [p.clone() for p in pristine]
-    conns = [c for c, _, _ in cases]
+    pristine = torch.from_numpy(marker_np).to(dev)
+    work = pristine.clone()
     handle = iwpp.Handle(local)
     lib = iwpp.load()
     stream = torch.cuda.Stream(dev)
     sptr = stream.cuda_stream
     vcode = iwpp._variant(variant)
-    cfg = iwpp.Config.make(tile_rows=args.tile_rows) if args.tile_rows else None
-    cfgp = __import__("ctypes").byref(cfg) if cfg is not None else None
 
-    def step(ev_pairs=None):
-        for i in range(len(cases)):
-            work[i].copy_(pristine[i], non_blocking=True)
-            if ev_pairs is not None:
-                ev_pairs[i][0].record(stream)
-            st = lib.iwpp_reconstruct_async(handle.ptr, work[i].data_ptr(), mask.data_ptr(), W, W, W, H, 0, conns[i],
-                                            vcode, cfgp, sptr)
-            if st != 0:
-                raise iwpp.IwppError(st, "iwpp_reconstruct_async")
-            if ev_pairs is not None:
-                ev_pairs[i][1].record(stream)
+    # the untuned default once, then the autotuner once for this image class
+    # (its winner goes to the tuning table that the default calls below read)
+    with torch.cuda.stream(stream):
+        st_untuned = iwpp.reconstruct(work, mask, connectivity=8, variant=variant, handle=handle, stream=stream)
+        work.copy_(pristine)
+        tuned = iwpp.autotune([(work, mask, 8)], variant=variant, repeats=1, handle=handle, stream=stream)
+    torch.cuda.synchronize()
+
+    def step(ev_pair=None):
+        work.copy_(pristine, non_blocking=True)
+        if ev_pair is not None:
+            ev_pair[0].record(stream)
+        st = lib.iwpp_reconstruct_async(handle.ptr, work.data_ptr(), mask.data_ptr(), W, W, W, H, 0, 8, vcode, None,
+                                        sptr)
+        if st != 0:
+            raise iwpp.IwppError(st, "iwpp_reconstruct_async")
+        if ev_pair is not None:
+            ev_pair[1].record(stream)
 
     with torch.cuda.stream(stream):
         for _ in range(max(args.warmup, 3)):
             step()
         stream.synchronize()
-        # bit-exact check of the warm-up results against the oracle
-        results = [w.cpu().numpy() for w in work]
-    cpu_res, cpu_secs = (None, None)
-    if rank == 0 and not args.no_cpu:
-        cpu_res, cpu_secs = cpu_oracle_cases(mask_np, cases, 1)
-    bitexact = None
-    if cpu_res is not None:
-        bitexact = all(np.array_equal(a, b) for a, b in zip(results, cpu_res))
+        result = work.cpu().numpy()
+    fixed_point_ok = iwpp.fixed_point_violations(work, mask, 8) == 0
 
     # ---- device-resident timed region
     clocks = ClockSampler(local)
-    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in cases]
-          for _ in range(args.steps)]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if world > 1:
         torch.distributed.barrier()
@@ -571,15 +691,18 @@ def run_ours(args):
     torch.cuda.synchronize()
     clock_info = clocks.stop()
     elapsed_ms = t_start.elapsed_time(t_end)
-    recon_ms = [a.elapsed_time(b) for row in ev for (a, b) in row]
+    recon_ms = [a.elapsed_time(b) for a, b in ev]
     if world > 1:
         elapsed_ms = max_over_ranks(elapsed_ms, dev)
         torch.distributed.barrier()
-    value = whole_job_gpx(world, px_step, args.steps, elapsed_ms)
+    value = whole_job_gpx(world, px, args.steps, elapsed_ms)
+    last = iwpp.Stats()
+    if lib.iwpp_handle_sync(handle.ptr, __import__("ctypes").byref(last)) != 0:
+        raise iwpp.IwppError(last.status, "iwpp_handle_sync")
+    timed_ok = bool(np.array_equal(work.cpu().numpy(), result))
 
-    # ---- serving sub-result first: the host-to-device path of a shared box
-    # slows down for a while after heavy copy traffic such as the end-to-end
-    # legs below
+    # ---- serving sub-result before the copy-heavy end-to-end legs: the
+    # host-to-device path of a shared box slows down for a while after them
     served = None
     if rank == 0 and not args.no_extras:
         try:
@@ -588,128 +711,117 @@ def run_ours(args):
             served = {"error": f"{type(exc).__name__}: {exc}"}
 
     # ---- end to end: pinned host buffers in, host buffers out, every copy
-    # inside the timed region.  `e2e`: each image through the per-image C-ABI
-    # call (iwpp_reconstruct_async) with its H2D and D2H copies on their own
-    # streams, double-buffered, so copies of the next / previous image
-    # overlap the reconstruction of this one.  `sync_call`: the same through
-    # the synchronous call, copies and reconstruction back to back.
-    e2e = None
-    if rank == 0 or world > 1:
-        host_m = [torch.from_numpy(m).pin_memory() for _, _, m in cases]
-        host_k = torch.from_numpy(mask_np).pin_memory()
-        host_out = [torch.empty(h.shape, dtype=h.dtype, pin_memory=True) for h in host_m]
-        dm = torch.empty((H, W), dtype=torch.uint8, device=dev)
-        dk = torch.empty((H, W), dtype=torch.uint8, device=dev)
+    # inside the timed region, through the per-image C-ABI call; copies on
+    # their own streams, two device buffer sets, so the next step's H2D and
+    # the previous step's D2H overlap this step's reconstruction
+    host_m = torch.from_numpy(marker_np).pin_memory()
+    host_k = torch.from_numpy(mask_np).pin_memory()
+    host_out = [torch.empty((H, W), dtype=torch.uint8, pin_memory=True) for _ in range(2)]
+    s_in, s_run, s_out = (torch.cuda.Stream(dev) for _ in range(3))
+    dmb = [torch.empty((H, W), dtype=torch.uint8, device=dev) for _ in range(2)]
+    dkb = [torch.empty((H, W), dtype=torch.uint8, device=dev) for _ in range(2)]
+    ev_in = [torch.cuda.Event() for _ in range(2)]
+    ev_run = [torch.cuda.Event() for _ in range(2)]
+    ev_out = [torch.cuda.Event() for _ in range(2)]
+    for e in ev_out:
+        e.record(s_out)
 
-        def sync_step():
-            for i in range(len(cases)):
-                dm.copy_(host_m[i], non_blocking=True)
-                dk.copy_(host_k, non_blocking=True)
-                iwpp.reconstruct(dm, dk, connectivity=conns[i], variant=variant, config=cfg, handle=handle)
-                host_out[i].copy_(dm, non_blocking=True)
-            torch.cuda.current_stream().synchronize()
+    def e2e_step(k, finish):
+        b = k & 1
+        with torch.cuda.stream(s_in):
+            s_in.wait_event(ev_out[b])  # buffer b's previous result is home
+            dmb[b].copy_(host_m, non_blocking=True)
+            dkb[b].copy_(host_k, non_blocking=True)
+            ev_in[b].record(s_in)
+        s_run.wait_event(ev_in[b])
+        st = lib.iwpp_reconstruct_async(handle.ptr, dmb[b].data_ptr(), dkb[b].data_ptr(), W, W, W, H, 0, 8, vcode,
+                                        None, s_run.cuda_stream)
+        if st != 0:
+            raise iwpp.IwppError(st, "iwpp_reconstruct_async")
+        ev_run[b].record(s_run)
+        with torch.cuda.stream(s_out):
+            s_out.wait_event(ev_run[b])
+            host_out[b].copy_(dmb[b], non_blocking=True)
+            ev_out[b].record(s_out)
+        if finish:
+            s_out.synchronize()
+            st = lib.iwpp_handle_sync(handle.ptr, None)
+            if st != 0:
+                raise iwpp.IwppError(st, "iwpp_handle_sync")
 
-        s_in, s_run, s_out = (torch.cuda.Stream(dev) for _ in range(3))
-        dmb = [torch.empty((H, W), dtype=torch.uint8, device=dev) for _ in range(2)]
-        dkb = [torch.empty((H, W), dtype=torch.uint8, device=dev) for _ in range(2)]
-        ev_in = [torch.cuda.Event() for _ in range(2)]
-        ev_run = [torch.cuda.Event() for _ in range(2)]
-        ev_out = [torch.cuda.Event() for _ in range(2)]
-        for e in ev_out:
-            e.record(s_out)
-
-        def pipelined_step(finish=True):
-            for i in range(len(cases)):
-                b = i & 1
-                with torch.cuda.stream(s_in):
-                    s_in.wait_event(ev_out[b])  # buffer b's previous result is home
-                    dmb[b].copy_(host_m[i], non_blocking=True)
-                    dkb[b].copy_(host_k, non_blocking=True)
-                    ev_in[b].record(s_in)
-                s_run.wait_event(ev_in[b])
-                st = lib.iwpp_reconstruct_async(handle.ptr, dmb[b].data_ptr(), dkb[b].data_ptr(), W, W, W, H, 0,
-                                                conns[i], vcode, cfgp, s_run.cuda_stream)
-                if st != 0:
-                    raise iwpp.IwppError(st, "iwpp_reconstruct_async")
-                ev_run[b].record(s_run)
-                with torch.cuda.stream(s_out):
-                    s_out.wait_event(ev_run[b])
-                    host_out[i].copy_(dmb[b], non_blocking=True)
-                    ev_out[b].record(s_out)
-            if finish:  # else the next step's copies overlap this step's tail
-                s_out.synchronize()
-                st = lib.iwpp_handle_sync(handle.ptr, None)
-                if st != 0:
-                    raise iwpp.IwppError(st, "iwpp_handle_sync")
-
-        e2e_steps_used = min(args.steps, 60)  # bounded copy volume; the rate is per step
-
-        def timed(step_fn, overlap_steps):
-            for _ in range(max(args.warmup, 3)):
-                step_fn()
-            ok = all(np.array_equal(host_out[i].numpy(), results[i]) for i in range(len(cases)))
-            for o in host_out:
-                o.zero_()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            for k in range(e2e_steps_used):
-                if overlap_steps:
-                    step_fn(finish=k == e2e_steps_used - 1)
-                else:
-                    step_fn()
-            secs = time.perf_counter() - t0
-            ok = ok and all(np.array_equal(host_out[i].numpy(), results[i]) for i in range(len(cases)))
-            return world * px_step * e2e_steps_used / secs / 1e9, ok
-
-        sync_value, sync_ok = timed(sync_step, False)
-        pipe_value, pipe_ok = timed(pipelined_step, True)
-        e2e_steps = e2e_steps_used
-        e2e = {"value": pipe_value, "unit": UNIT,
-               "h2d_bytes_per_step": len(cases) * 2 * W * H, "d2h_bytes_per_step": len(cases) * W * H,
-               "path": "iwpp_reconstruct_async per image, H2D / reconstruction / D2H on three streams, "
-                       "steps back to back (one host wait at the end of the timed region)",
-               "bitexact_vs_device_path": pipe_ok, "steps": e2e_steps,
-               "sync_call": {"value": sync_value, "unit": UNIT, "bitexact_vs_device_path": sync_ok,
-                             "path": "synchronous iwpp_reconstruct per image, copies before and after"}}
+    for k in range(max(args.warmup, 3)):
+        e2e_step(k, k == max(args.warmup, 3) - 1)
+    e2e_steps = min(args.steps, 30)  # bounded copy volume; the rate is per step
+    for o in host_out:
+        o.zero_()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        e2e_step(k, k == e2e_steps - 1)
+    e2e_secs = time.perf_counter() - t0
+    if world > 1:
+        e2e_secs = max_over_ranks(e2e_secs, dev)
+    e2e_ok = all(np.array_equal(o.numpy(), result) for o in host_out)
+    e2e = {"value": whole_job_gpx(world, px, e2e_steps, e2e_secs * 1e3), "unit": UNIT,
+           "h2d_bytes_per_step": 2 * W * H, "d2h_bytes_per_step": W * H,
+           "path": "iwpp_reconstruct_async per step from pinned host buffers: H2D / reconstruction / D2H on three "
+                   "streams, two device buffer sets, steps back to back (one host wait at the end)",
+           "steps": e2e_steps, "bitexact_vs_device_path": e2e_ok}
+    del dmb, dkb
+    torch.cuda.empty_cache()
 
     if rank != 0:
+        handle.close()
         if world > 1:
             torch.distributed.destroy_process_group()
         return 0
+    extras = {}
+    if not args.no_extras:
+        for key, fn in (("config1", bench_config1), ("batched", None), ("spiral_types", bench_spiral_types)):
+            try:
+                extras[key] = fn(args, dev, variant, handle) if fn else bench_batched(args, dev, variant)
+            except Exception as exc:  # reported in the line, the headline stands
+                extras[key] = {"error": f"{type(exc).__name__}: {exc}"}
+    cpu = None
+    bitexact = None
+    if oracle_fut is not None:
+        ref, cpu_secs = oracle_fut.result()
+        bitexact = bool(np.array_equal(result, ref))
+        cpu = {"value": px / cpu_secs / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "the same 16384x16384 uint8 spiral reconstruction once, oracle (Vincent 1993 hybrid), one "
+                         f"host thread ({cpu_secs:.1f} s)"}
+    oracle_ex.shutdown()
     peak, peak_kind = peak_hbm()
     mean_recon_ms = sum(recon_ms) / len(recon_ms)
     achieved = bytes_per_recon / (mean_recon_ms / 1e3) / 1e9
-    traffic = traffic_from_profile()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "config": {"workload": WORKLOAD, "variant": variant,
-                   "tile_rows": args.tile_rows or ("default: %d" % (32 if iwpp.tile_count(W, H, 0, 0) ==
-                                                                      iwpp.tile_count(W, H, 0, 32) else 64)),
-                   "l2": "inputs larger than L2: 6 working + 6 pristine markers + mask = 218 MB per step",
+                   "autotuned": {k_: tuned[k_] for k_ in ("tile_rows", "solver", "init_passes", "front_passes")},
+                   "l2": "inputs larger than L2: working + pristine marker + mask = 805 MB per step",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-        "bitexact": bitexact,
+        "bitexact": bitexact, "bitexact_timed_steps": timed_ok, "fixed_point": fixed_point_ok,
+        "untuned_ms": st_untuned.device_ms,
+        "reconstruction": {"tiles": last.tiles, "visits": last.visits, "front_sweeps": last.front_sweeps,
+                           "launches": last.launches, "corridor_pixels": n_corridor},
         "e2e": e2e,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "iwpp::engine_kernel (persistent tile engine) + its init kernel",
+                     "frac": achieved / peak, "traffic": traffic_from_profile("headline"), "peak_source": peak_kind,
+                     "kernel": "one reconstruction: all of libiwpp's kernels of the call (front passes, check, "
+                               "engine init, tile engine), events around the call on its stream",
                      "algorithmic_bytes_per_launch": bytes_per_recon, "mean_launch_ms": mean_recon_ms},
-        "cpu_baseline": None if cpu_secs is None else {
-            "value": px_step / cpu_secs / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": "the same six 4096x4096 uint8 reconstructions, oracle (Vincent 1993 hybrid), one thread"},
+        "cpu_baseline": cpu,
         "clocks": clock_info,
-        "gpu_launches": args.steps * len(cases) * 2,
+        "gpu_launches": args.steps * int(last.launches),
     }
     handle.close()
     if served is not None:
         line["served"] = served
-    if not args.no_extras:
-        for key, fn in (("batched", bench_batched), ("spiral", bench_spiral)):
-            try:
-                line[key] = fn(args, dev, variant)
-            except Exception as exc:  # reported in the line, the headline stands
-                line[key] = {"error": f"{type(exc).__name__}: {exc}"}
+    line.update(extras)
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -719,14 +831,13 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--variant", default="async", choices=["mutex", "double", "unique", "async"])
-    ap.add_argument("--tile-rows", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline / bit-exact checks")
     ap.add_argument("--no-extras", action="store_true",
-                    help="only the headline line (no batched / served / spiral sub-results)")
+                    help="only the headline line (no config1 / batched / served / spiral-type sub-results)")
     ap.add_argument("--served-requests", type=int, default=4000)
     ap.add_argument("--lanes", type=int, default=3)
     ap.add_argument("--spiral-reps", type=int, default=3)

@@ -102,6 +102,8 @@ typedef struct iwpp_stats {
      * taking an entry), tile fetch, processing (sweeps), dump (write-back and
      * neighbour detection), queue write (state updates and insertions). */
     long long phase_cycles[5];
+    long long launches;    /* kernels this library launched for the job */
+    long long front_sweeps; /* directional sweeps the front passes ran (0 without them) */
 } iwpp_stats;
 
 /* One image of a batch. */

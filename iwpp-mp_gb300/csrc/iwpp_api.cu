@@ -493,6 +493,7 @@ struct iwpp_handle_s {
     long long last_tiles = 0;
     int last_variant = IWPP_QUEUE_UNIQUE;
     int last_launch_status = IWPP_OK;
+    int last_launches = 0;
     bool timed = false;
     std::mutex mu;
 };
@@ -507,6 +508,7 @@ struct iwpp_plan_s {
     cudaStream_t last_stream = nullptr;
     long long tiles = 0;
     int variant = IWPP_QUEUE_UNIQUE;
+    int launches = 0;
 };
 
 namespace {
@@ -544,7 +546,15 @@ int check_device(int device) {
 
 // Enqueues a prepared job on `s` into workspace `ws`.
 int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool use_events, cudaEvent_t ev0,
-                cudaEvent_t ev1, bool upload_descs, HostStaging* hs = nullptr) {
+                cudaEvent_t ev1, bool upload_descs, HostStaging* hs = nullptr, int* launches = nullptr) {
+    int nl = 0;  // kernels launched
+    struct Count {
+        int* out;
+        int* n;
+        ~Count() {
+            if (out) *out = *n;
+        }
+    } count_out{launches, &nl};
     const bool two = job.variant == IWPP_QUEUE_DOUBLE || job.variant == IWPP_QUEUE_UNIQUE;
     const long long cap = job_queue_capacity(job);
     const Layout l = job_layout(job);
@@ -591,6 +601,7 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
         for (const auto& d : job.descs) {
             e = launch_clip(d, s);
             if (e != cudaSuccess) return cuda_status(e);
+            ++nl;
         }
     for (int p = 0; p < job.cfg.init_passes; ++p)
         for (const auto& d : job.descs)
@@ -602,11 +613,12 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
                 static const int order[4] = {0, 1, 2, 3};
                 ImgDesc dv = d;
                 dv.conn = 4;
-                e = launch_sweep(dv, order[dir], s, base + l.off_sweep);
+                e = launch_sweep(dv, order[dir], s, base + l.off_sweep, &nl);
                 if (e != cudaSuccess) return cuda_status(e);
             }
     e = engine_launch_init(a, job.variant, s);
     if (e != cudaSuccess) return cuda_status(e);
+    ++nl;
     if (job.G > 0) {
         LaunchInfo li;
         e = engine_prepare(job.variant, job.tile_rows, device, &li);
@@ -618,13 +630,14 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
         if (grid < 1) grid = 1;
         e = engine_launch(a, job.variant, job.tile_rows, (int)grid, s);
         if (e != cudaSuccess) return cuda_status(e);
+        ++nl;
     }
     if (use_events) cudaEventRecord(ev1, s);
     return IWPP_OK;
 }
 
 int read_stats(Ctrl* host_ctrl, const Workspace& ws, cudaStream_t s, long long tiles, int variant,
-               iwpp_stats* out, float ms) {
+               iwpp_stats* out, float ms, int launches = 0) {
     cudaError_t e = cudaMemcpyAsync(host_ctrl, ws.base, sizeof(Ctrl), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_status(e);
@@ -643,6 +656,8 @@ int read_stats(Ctrl* host_ctrl, const Workspace& ws, cudaStream_t s, long long t
         out->device_ms = ms;
         out->row_steps = (long long)host_ctrl->row_steps;
         for (int i = 0; i < 5; ++i) out->phase_cycles[i] = (long long)host_ctrl->phase[i];
+        out->launches = launches;
+        out->front_sweeps = (long long)host_ctrl->front_sweeps;
     }
     return st;
 }
@@ -696,8 +711,9 @@ int run_job_sync(iwpp_handle h, const iwpp_image* imgs, int n, int variant, cons
     cudaGetDevice(&prev_dev);
     if (prev_dev != h->device) cudaSetDevice(h->device);
     Job job;
+    int nl = 0;
     rc = build_job(job, imgs, n, variant, cfg, s, STAGE_ASYNC);
-    if (rc == IWPP_OK) rc = enqueue_job(job, h->ws, s, h->device, true, h->ev0, h->ev1, true, &h->staging);
+    if (rc == IWPP_OK) rc = enqueue_job(job, h->ws, s, h->device, true, h->ev0, h->ev1, true, &h->staging, &nl);
     const int rc_stage = finish_staging(job, s);
     if (rc == IWPP_OK) {
         float ms = 0.f;
@@ -706,7 +722,7 @@ int run_job_sync(iwpp_handle h, const iwpp_image* imgs, int n, int variant, cons
             rc = cuda_status(e);
         else {
             cudaEventElapsedTime(&ms, h->ev0, h->ev1);
-            rc = read_stats(h->host_ctrl, h->ws, s, job.G, job.variant, stats, ms);
+            rc = read_stats(h->host_ctrl, h->ws, s, job.G, job.variant, stats, ms, nl);
         }
     } else {
         cudaStreamSynchronize(s);
@@ -829,8 +845,9 @@ int iwpp_reconstruct_batch_async(iwpp_handle h, const iwpp_image* images, int n,
     if (prev_dev != h->device) cudaSetDevice(h->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     Job job;
+    int nl = 0;
     int rc = build_job(job, images, n, variant, cfg, s, STAGE_ASYNC);
-    if (rc == IWPP_OK) rc = enqueue_job(job, h->ws, s, h->device, true, h->ev0, h->ev1, true, &h->staging);
+    if (rc == IWPP_OK) rc = enqueue_job(job, h->ws, s, h->device, true, h->ev0, h->ev1, true, &h->staging, &nl);
     const int rc2 = finish_staging(job, s);
     if (rc == IWPP_OK) rc = rc2;
     if (rc == IWPP_OK && h->ws.base) {
@@ -844,6 +861,7 @@ int iwpp_reconstruct_batch_async(iwpp_handle h, const iwpp_image* images, int n,
     h->last_tiles = job.G;
     h->last_variant = job.variant;
     h->last_launch_status = rc;
+    h->last_launches = nl;
     h->timed = job.G > 0;
     if (prev_dev != h->device) cudaSetDevice(prev_dev);
     return set_last(rc);
@@ -880,6 +898,8 @@ int iwpp_handle_sync(iwpp_handle h, iwpp_stats* stats) {
         stats->device_ms = ms;
         stats->row_steps = (long long)c.row_steps;
         for (int i = 0; i < 5; ++i) stats->phase_cycles[i] = (long long)c.phase[i];
+        stats->launches = h->last_launches;
+        stats->front_sweeps = (long long)c.front_sweeps;
     }
     return set_last(st);
 }
@@ -943,7 +963,8 @@ int iwpp_plan_create(iwpp_plan* out, iwpp_handle h, const iwpp_image* images, in
                                           cudaMemcpyDeviceToDevice, cs);
             }
             rc = cuda_status(e);
-            if (rc == IWPP_OK) rc = enqueue_job(job, p->ws, cs, h->device, false, nullptr, nullptr, false);
+            if (rc == IWPP_OK)
+                rc = enqueue_job(job, p->ws, cs, h->device, false, nullptr, nullptr, false, nullptr, &p->launches);
             for (const auto& st : p->staged) {
                 const size_t row = (size_t)st.w * bpp_of(st.dtype);
                 if (rc == IWPP_OK)
@@ -995,6 +1016,8 @@ int iwpp_plan_sync(iwpp_plan p, iwpp_stats* stats) {
         stats->device_ms = 0.0;
         stats->row_steps = (long long)c.row_steps;
         for (int i = 0; i < 5; ++i) stats->phase_cycles[i] = (long long)c.phase[i];
+        stats->launches = p->launches;
+        stats->front_sweeps = (long long)c.front_sweeps;
     }
     return set_last(st);
 }

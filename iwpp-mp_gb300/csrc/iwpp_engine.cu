@@ -679,6 +679,7 @@ __global__ void engine_init_kernel(EngineArgs a, int variant) {
         c->pushes = 0ull;
         c->row_steps = 0ull;
         for (int i = 0; i < 5; ++i) c->phase[i] = 0ull;
+        if (!a.front) c->front_sweeps = 0ull;  // else the front passes' count stands
     }
 }
 

@@ -65,6 +65,7 @@ struct Ctrl {
     unsigned long long pushes;
     unsigned long long row_steps;
     unsigned long long phase[5];  // cycles: queue read, fetch, processing, dump, queue write
+    unsigned long long front_sweeps;  // directional sweeps run by the front passes
 };
 
 struct EngineArgs {
@@ -80,6 +81,7 @@ struct EngineArgs {
     int max_restarts;
     int solver;  // 0 automatic, 1 row sweeps, 2 passes
     int phantom;  // test hook: one unit of work that never arrives (every wait runs out)
+    int front;    // the front passes ran before this job's engine launch
 };
 
 }  // namespace iwpp
@@ -106,6 +108,8 @@ cudaError_t queue_selftest(const EngineArgs& a, int variant, int copies, unsigne
 // Whole-image sweep; 4-connected vertical sweeps of tall uint8 / uint16
 // images use `scratch` (sweep_scratch_bytes(d) bytes, nullable) to split the
 // columns into segments.
-cudaError_t launch_sweep(const ImgDesc& d, int direction, cudaStream_t s, void* scratch = nullptr);
+// `launches` (nullable) is incremented by the number of kernels launched.
+cudaError_t launch_sweep(const ImgDesc& d, int direction, cudaStream_t s, void* scratch = nullptr,
+                         int* launches = nullptr);
 size_t sweep_scratch_bytes(const ImgDesc& d);
 }  // namespace iwpp

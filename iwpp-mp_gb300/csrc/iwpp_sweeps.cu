@@ -561,7 +561,7 @@ cudaError_t launch_clip(const ImgDesc& d, cudaStream_t s) {
 }
 
 template <int DT>
-static void launch_sweep_t(const ImgDesc& d, int direction, cudaStream_t s, void* scratch) {
+static int launch_sweep_t(const ImgDesc& d, int direction, cudaStream_t s, void* scratch) {
     using P = Px<DT>;
     constexpr int TW = 32 * P::PPW;
     if (direction == 0 || direction == 2) {
@@ -570,6 +570,7 @@ static void launch_sweep_t(const ImgDesc& d, int direction, cudaStream_t s, void
             sweep_x_kernel<DT, true><<<blocks, 128, 0, s>>>(d);
         else
             sweep_x_kernel<DT, false><<<blocks, 128, 0, s>>>(d);
+        return 1;
     } else {
         const int strips = (d.W + TW - 1) / TW;
         const unsigned blocks = (unsigned)strips;
@@ -597,6 +598,7 @@ static void launch_sweep_t(const ImgDesc& d, int direction, cudaStream_t s, void
                     sweep_y4i_kernel<true, 2><<<grid, 32, 0, s>>>(d, nullptr, nullptr, in);
                 else
                     sweep_y4i_kernel<false, 2><<<grid, 32, 0, s>>>(d, nullptr, nullptr, in);
+                return 3;
             } else if (down) {
                 sweep_y4i_kernel<true, 0><<<nblocks, 32, 0, s>>>(d, nullptr, nullptr, nullptr);
             } else {
@@ -622,23 +624,27 @@ static void launch_sweep_t(const ImgDesc& d, int direction, cudaStream_t s, void
                     sweep_y4n_kernel<NDT, true, 2><<<grid, 32, 0, s>>>(d, nullptr, nullptr, in);
                 else
                     sweep_y4n_kernel<NDT, false, 2><<<grid, 32, 0, s>>>(d, nullptr, nullptr, in);
+                return 3;
             } else if (down) {
                 sweep_y4n_kernel<NDT, true, 0><<<nblocks, 32, 0, s>>>(d, nullptr, nullptr, nullptr);
             } else {
                 sweep_y4n_kernel<NDT, false, 0><<<nblocks, 32, 0, s>>>(d, nullptr, nullptr, nullptr);
             }
         }
+        return 1;
     }
 }
 
-cudaError_t launch_sweep(const ImgDesc& d, int direction, cudaStream_t s, void* scratch) {
+cudaError_t launch_sweep(const ImgDesc& d, int direction, cudaStream_t s, void* scratch, int* launches) {
     if (d.W == 0 || d.H == 0) return cudaSuccess;
+    int n;
     if (d.dtype == DT_U8)
-        launch_sweep_t<DT_U8>(d, direction, s, scratch);
+        n = launch_sweep_t<DT_U8>(d, direction, s, scratch);
     else if (d.dtype == DT_U16)
-        launch_sweep_t<DT_U16>(d, direction, s, scratch);
+        n = launch_sweep_t<DT_U16>(d, direction, s, scratch);
     else
-        launch_sweep_t<DT_I32>(d, direction, s, scratch);
+        n = launch_sweep_t<DT_I32>(d, direction, s, scratch);
+    if (launches) *launches += n;
     return cudaGetLastError();
 }
 
