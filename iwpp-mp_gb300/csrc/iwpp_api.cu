@@ -16,6 +16,7 @@
 
 #include "iwpp.h"
 #include "iwpp_engine.cuh"
+#include "iwpp_front.cuh"
 #include "iwpp_tune.h"
 
 using namespace iwpp;
@@ -202,11 +203,14 @@ struct Workspace {
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 struct Layout {
-    size_t off_imgs, off_tmaps, off_state, off_q0, off_q1, off_sweep, total;
+    size_t off_imgs, off_tmaps, off_state, off_q0, off_q1, off_sweep, off_list, total;
 };
 
-// sweep_bytes: scratch of the whole-image sweeps run before the engine
-Layout layout_for(long long n_imgs, long long G, long long cap, bool two_queues, size_t sweep_bytes = 0) {
+// sweep_bytes: scratch of the whole-image sweeps or front passes run before
+// the engine; seed_list: room for the engine's seed list after front passes
+// (G ids and their count)
+Layout layout_for(long long n_imgs, long long G, long long cap, bool two_queues, size_t sweep_bytes = 0,
+                  bool seed_list = false) {
     Layout l;
     l.off_imgs = align_up(sizeof(Ctrl), 256);
     l.off_tmaps = align_up(l.off_imgs + (size_t)n_imgs * sizeof(ImgDesc), 256);
@@ -214,9 +218,14 @@ Layout layout_for(long long n_imgs, long long G, long long cap, bool two_queues,
     l.off_q0 = align_up(l.off_state + (size_t)G * 4u, 256);
     l.off_q1 = align_up(l.off_q0 + (size_t)cap * 4u, 256);
     l.off_sweep = align_up(l.off_q1 + (two_queues ? (size_t)cap * 4u : 0u), 256);
-    l.total = align_up(l.off_sweep + sweep_bytes, 256);
+    l.off_list = align_up(l.off_sweep + sweep_bytes, 256);
+    l.total = align_up(l.off_list + (seed_list ? (size_t)(G + 1) * 4u : 0u), 256);
     return l;
 }
+
+// Sweeps the front passes may run (four per pass) before the tile engine
+// takes over whatever is left.
+constexpr int kFrontMaxSweeps = 4096;
 
 long long queue_capacity_for(int variant, long long G, long long requested) {
     long long cap;
@@ -267,14 +276,17 @@ long long job_queue_capacity(const Job& job) {
 // The workspace layout of a job (the same for direct calls and plans).
 Layout job_layout(const Job& job) {
     const bool two = job.variant == IWPP_QUEUE_DOUBLE || job.variant == IWPP_QUEUE_UNIQUE;
+    const bool front = job.cfg.front_passes == 1;
     size_t sweep = 0;
-    if (job.cfg.init_passes > 0)
-        for (const auto& d : job.descs) {
+    for (const auto& d : job.descs) {
+        if (job.cfg.init_passes > 0) {
             ImgDesc dv = d;
             dv.conn = 4;
             sweep = std::max(sweep, sweep_scratch_bytes(dv));
         }
-    return layout_for((long long)job.descs.size(), job.G, job_queue_capacity(job), two, sweep);
+        if (front) sweep = std::max(sweep, front_scratch_bytes(d));
+    }
+    return layout_for((long long)job.descs.size(), job.G, job_queue_capacity(job), two, sweep, front);
 }
 
 // How images whose rows are not 4-byte aligned are handled.
@@ -574,6 +586,14 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
     a.max_restarts = job.cfg.max_restarts;
     a.solver = job.cfg.solver;
     a.phantom = job.cfg.phantom_work;
+    const bool front = job.cfg.front_passes == 1 && job.G > 0;
+    unsigned* seed_list = reinterpret_cast<unsigned*>(base + l.off_list);
+    unsigned* seed_count = seed_list + job.G;
+    if (front) {
+        a.front = 1;
+        a.init_list = seed_list;
+        a.init_count = seed_count;
+    }
 
     cudaError_t e = cudaSuccess;
     if (upload_descs && !job.descs.empty()) {
@@ -603,6 +623,22 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
             if (e != cudaSuccess) return cuda_status(e);
             ++nl;
         }
+    if (front) {
+        // Front passes over each image, then the check that seeds the tile
+        // engine with the tiles still holding a pixel a neighbour can raise.
+        // The job's error word and sweep count are zeroed first: the passes
+        // write them and the engine's initialisation keeps them.
+        Ctrl* c = a.ctrl;
+        e = cudaMemsetAsync(&c->error, 0, sizeof(c->error), s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(&c->front_sweeps, 0, sizeof(c->front_sweeps), s);
+        for (size_t i = 0; i < job.descs.size() && e == cudaSuccess; ++i)
+            e = launch_front(job.descs[i], base + l.off_sweep, &c->error, &c->front_sweeps, kFrontMaxSweeps,
+                             a.timeout_ns, device, s, &nl);
+        if (e == cudaSuccess) e = cudaMemsetAsync(seed_count, 0, sizeof(unsigned), s);
+        for (size_t i = 0; i < job.descs.size() && e == cudaSuccess; ++i)
+            e = launch_seed(job.descs[i], a.state, seed_list, seed_count, s, &nl);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
     for (int p = 0; p < job.cfg.init_passes; ++p)
         for (const auto& d : job.descs)
             for (int dir = 0; dir < 4; ++dir) {
@@ -1183,10 +1219,19 @@ int iwpp_autotune(iwpp_handle h, const iwpp_image* images, int n, int variant, i
                 c.init_passes = 0;
                 consider(c, th == dflt_th && solver == 0);
             }
-        // stage 2: initial whole-image raster / anti-raster passes, doubling
-        // while they pay (long corridors want one pass per turn of the
-        // front), stopping at the first count that does not beat the best
+        // stage 2: front passes (directional sweeps restricted to the tiles
+        // that changed, until nothing changes) before the tile engine, with
+        // the best tile height and solver; long propagation paths want them
         if (best_ms >= 0.0) {
+            iwpp_config c = best;
+            c.front_passes = 1;
+            consider(c, false);
+        }
+        // stage 3: else a fixed number of initial whole-image raster /
+        // anti-raster passes, doubling while they pay (long corridors want
+        // one pass per turn of the front), stopping at the first count that
+        // does not beat the best
+        if (best_ms >= 0.0 && best.front_passes != 1) {
             const iwpp_config base = best;
             for (int ip = 1; ip <= 64; ip *= 2) {
                 iwpp_config c = base;
@@ -1196,7 +1241,7 @@ int iwpp_autotune(iwpp_handle h, const iwpp_image* images, int n, int variant, i
                 if (!(best_ms < before)) break;
             }
         }
-        // stage 3: queue capacity, for the queues whose capacity is free
+        // stage 4: queue capacity, for the queues whose capacity is free
         if (best_ms >= 0.0 && (v == IWPP_QUEUE_MUTEX || v == IWPP_QUEUE_DOUBLE)) {
             const iwpp_config base = best;
             for (int mult : {1, 16}) {

@@ -11,6 +11,12 @@ __device__ __forceinline__ int ld_volatile(const int* p) { return *(const volati
 
 __device__ __forceinline__ void set_error(Ctrl* c, unsigned code) { atomicCAS(&c->error, 0u, code); }
 
+// Async ring: positions below this are the job's initial entries (every
+// tile, or the seed list after front passes), the rest map to ring slots.
+__device__ __forceinline__ unsigned ring_base(const EngineArgs& a) {
+    return a.init_list ? ld_volatile(&a.ctrl->ninit) : a.G;
+}
+
 // Image of global tile g: the last image whose tile_base <= g.
 __device__ __forceinline__ int find_image(const EngineArgs& a, unsigned g) {
     int lo = 0, hi = a.nimg - 1;
@@ -138,7 +144,7 @@ __device__ void push_entries(const EngineArgs& a, bool want, unsigned gn, int la
         }
         base = __shfl_sync(FULL, base, 0);
         if (want) {
-            const unsigned slot = (base + (unsigned)rank - a.G) % a.cap;
+            const unsigned slot = (base + (unsigned)rank - ring_base(a)) % a.cap;
             const long long t0 = globaltimer_ns();
             unsigned spins = 0;
             // the slot's previous occupant has normally been taken long ago
@@ -434,24 +440,26 @@ __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
 }
 
 // ------------------------------------------------------- async worker
-// Ring positions 0..G-1 are the initial tiles (no storage); position p >= G
-// lives in slot (p - G) % cap.  A warp claims the next position with one
+// Ring positions 0..n0-1 are the initial tiles (no storage: every tile in
+// id order, or the seed list after front passes); position p >= n0 lives in
+// slot (p - n0) % cap.  A warp claims the next position with one
 // atomicAdd and waits for a producer to fill it.  Every filled position is
 // claimed by exactly one warp, and when `pending` (filled, unfinished
 // entries) reaches zero no producer is left, so waiting warps leave.
 template <int TH>
 __device__ void async_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, WarpCounters& cnt, unsigned& phase) {
+    const unsigned n0 = ring_base(a);
     for (;;) {
         const long long qr0 = clock64();
         unsigned p = 0u;
         if (lane == 0) p = atomicAdd(&a.ctrl->ahead, 1u);
         p = __shfl_sync(FULL, p, 0);
-        unsigned g = p;
-        if (p >= a.G) {
+        unsigned g = a.init_list && p < n0 ? __ldcg(&a.init_list[p]) : p;
+        if (p >= n0) {
             int verdict = 0;  // 0 got an entry, 1 exit
             unsigned v = 0u;
             if (lane == 0) {
-                const unsigned slot = (p - a.G) % a.cap;
+                const unsigned slot = (p - n0) % a.cap;
                 long long idle_since = globaltimer_ns();
                 unsigned idle_progress = ld_volatile(&a.ctrl->progress);
                 unsigned ns = 32, spins = 0;
@@ -639,37 +647,45 @@ __global__ void __launch_bounds__(kWarps * 32) engine_kernel(EngineArgs a) {
 // Job initialisation: every tile DIRTY; round 0 (double / unique) is the
 // virtual list of all tiles; the mutex stack holds every tile so that the
 // first pops come out in raster order (IWPP MP/src/globalQueue.cu:83-97,
-// initFillGlobalQueue).
+// initFillGlobalQueue).  After front passes the seed check has set the tile
+// states and listed the tiles to start from: the mutex stack and the first
+// round's read queue are that list, the async ring starts from it; the
+// passes' error and sweep count stand.
 __global__ void engine_init_kernel(EngineArgs a, int variant) {
     const unsigned stride = gridDim.x * blockDim.x;
+    const bool seeded = a.init_list != nullptr;
+    unsigned n0 = a.G;
+    if (seeded) n0 = min(*(const volatile unsigned*)a.init_count, a.G);
     for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < a.G; g += stride) {
-        a.state[g] = ST_DIRTY | ST_SIDES;
-        if (variant == VAR_MUTEX && g < a.cap) a.q0[g] = a.G - 1u - g;
+        if (!seeded) a.state[g] = ST_DIRTY | ST_SIDES;
+        if (variant == VAR_MUTEX && g < a.cap) a.q0[g] = seeded ? (g < n0 ? a.init_list[g] : 0u) : a.G - 1u - g;
+        if ((variant == VAR_DOUBLE || variant == VAR_UNIQUE) && seeded && g < n0 && g < a.cap) a.q0[g] = a.init_list[g];
     }
     if (variant == VAR_ASYNC)
         for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < a.cap; i += stride) a.q0[i] = 0u;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         Ctrl* c = a.ctrl;
-        c->rn = a.G;
+        c->rn = n0;
         c->wn = 0u;
         c->rcur = 0u;
         c->qsel = 0u;
-        c->vfull = 1u;
-        c->done = a.G == 0u ? 1u : 0u;
-        c->overflow = a.G > a.cap && variant == VAR_MUTEX ? 1u : 0u;
+        c->vfull = seeded ? 0u : 1u;
+        c->done = n0 == 0u ? 1u : 0u;
+        c->overflow = n0 > a.cap && variant == VAR_MUTEX ? 1u : 0u;
         c->restarts = 0u;
         c->rounds = 0u;
         c->bar_count = 0u;
         c->bar_gen = 0u;
-        c->error = 0u;
+        if (!a.front) c->error = 0u;  // else the front passes' error stands
         c->lock_next = 0u;
         c->lock_serving = 0u;
-        c->top = (int)(a.G < a.cap ? a.G : a.cap);
-        c->pending = (int)(a.G < a.cap ? a.G : a.cap);
+        c->top = (int)(n0 < a.cap ? n0 : a.cap);
+        c->pending = (int)(n0 < a.cap ? n0 : a.cap);
         c->progress = 0u;
         c->ahead = 0u;
-        c->atail = a.G;
-        if (variant == VAR_ASYNC) c->pending = (int)a.G;
+        c->atail = n0;
+        c->ninit = n0;
+        if (variant == VAR_ASYNC) c->pending = (int)n0;
         // test hook: one pending entry that nobody inserts or finishes, so
         // the waiting warps never see the job end and their bounded waits
         // run out (the round-based queues stall at their barrier instead)

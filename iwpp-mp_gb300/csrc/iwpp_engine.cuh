@@ -66,6 +66,7 @@ struct Ctrl {
     unsigned long long row_steps;
     unsigned long long phase[5];  // cycles: queue read, fetch, processing, dump, queue write
     unsigned long long front_sweeps;  // directional sweeps run by the front passes
+    unsigned ninit;     // initial entries (every tile, or the seed list after front passes)
 };
 
 struct EngineArgs {
@@ -82,6 +83,11 @@ struct EngineArgs {
     int solver;  // 0 automatic, 1 row sweeps, 2 passes
     int phantom;  // test hook: one unit of work that never arrives (every wait runs out)
     int front;    // the front passes ran before this job's engine launch
+    // After front passes: the tiles to start from (ids) and their count (a
+    // device counter); nullptr: every tile, in id order.  The tile states
+    // were set by the seed check.
+    const unsigned* init_list;
+    const unsigned* init_count;
 };
 
 }  // namespace iwpp

@@ -1,0 +1,144 @@
+"""GPU parity of the front passes (iwpp_config.front_passes = 1): whole-image
+directional sweeps restricted to the tiles that changed, then the seed check
+and the tile engine from the tiles still violating a constraint.  Every
+result must equal the CPU oracle bit for bit, for every pixel type,
+connectivity and queue variant, on ragged and degenerate shapes, unclipped
+markers, padded pitches, batches and graph plans."""
+import numpy as np
+import pytest
+
+import iwpp
+import oracle
+from iwpp import synth
+
+pytestmark = pytest.mark.gpu
+
+VARIANTS = ["mutex", "double", "unique", "async"]
+NP = {0: np.uint8, 1: np.uint16, 2: np.int32}
+FRONT = dict(front_passes=1)
+
+
+def to_dev(a):
+    import torch
+    return torch.from_numpy(a.view(np.int16) if a.dtype == np.uint16 else a).cuda()
+
+
+def from_dev(t, dtype):
+    a = t.cpu().numpy()
+    return a.view(np.uint16) if dtype == np.uint16 else a
+
+
+def run(marker, mask, conn, variant="async", **cfg):
+    m, k = to_dev(marker), to_dev(mask)
+    st = iwpp.reconstruct(m, k, connectivity=conn, variant=variant, config=iwpp.Config.make(**FRONT, **cfg))
+    return from_dev(m, marker.dtype), st
+
+
+@pytest.mark.parametrize("dt", [0, 1, 2])
+@pytest.mark.parametrize("conn", [4, 8])
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_front_random_shapes(dt, conn, variant):
+    rng = np.random.default_rng(500 + 10 * dt + conn + len(variant))
+    shapes = [(1, 1), (1, 131), (131, 1), (3, 5), (64, 128), (65, 129), (200, 333), (513, 257), (130, 1029)]
+    for i, (h, w) in enumerate(shapes):
+        mask = synth.noise_mask(w, h, dt, 80 + i, 2.0, 3)
+        marker = synth.sparse_marker(mask, 9 + i, 0.01) if i % 3 == 0 else \
+            synth.hdome_marker(mask, int(rng.integers(5, 80)))
+        ref = oracle.reconstruct(marker, mask, conn)
+        out, st = run(marker, mask, conn, variant)
+        assert st.status == 0
+        assert np.array_equal(out, ref), (h, w, int((out != ref).sum()))
+        if h * w > 1000:
+            assert st.front_sweeps >= 4
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_front_spirals_and_config0(variant):
+    for dt in (0, 1, 2):
+        marker, mask, _ = synth.spiral_case(1024, 1024, dt, sigma=8.0, arm_pitch=32, nseeds=4)
+        ref = oracle.reconstruct(marker, mask, 8)
+        out, st = run(marker, mask, 8, variant)
+        assert np.array_equal(out, ref), (dt, int((out != ref).sum()))
+        # the corridor is carried by the passes: the engine only finishes
+        assert st.visits < st.tiles
+    marker, mask = synth.config0()
+    ref = oracle.reconstruct(marker, mask, 8)
+    out, _ = run(marker, mask, 8, variant)
+    assert np.array_equal(out, ref)
+
+
+@pytest.mark.parametrize("tile_rows", [32, 64])
+def test_front_unclipped_noise(tile_rows):
+    # raw noise with the marker above the mask at half of the pixels (no
+    # precondition), full value ranges (int32 negatives next to the border)
+    rng = np.random.default_rng(7 + tile_rows)
+    for dt in (0, 1, 2):
+        info = np.iinfo(NP[dt])
+        mask = rng.integers(info.min, info.max, (300, 700), dtype=np.int64).astype(NP[dt])
+        marker = rng.integers(info.min, info.max, (300, 700), dtype=np.int64).astype(NP[dt])
+        for conn in (4, 8):
+            ref = oracle.reconstruct(marker, mask, conn)
+            out, _ = run(marker, mask, conn, "async", tile_rows=tile_rows)
+            assert np.array_equal(out, ref), (dt, conn)
+
+
+def test_front_padded_pitch_and_unaligned_rows():
+    import torch
+    mask = synth.noise_mask(301, 197, 0, 3, 2.0, 4)
+    marker = synth.hdome_marker(mask, 25)
+    ref = oracle.reconstruct(marker, mask, 8)
+    # a 512-byte pitch (rows on 16-byte boundaries: tiles staged by cp.async)
+    # and a 308-byte pitch (4-byte aligned only: lane-word loads)
+    for pitch in (512, 308):
+        big_m = torch.full((197, pitch), 77, dtype=torch.uint8, device="cuda")
+        big_k = torch.full((197, pitch), 99, dtype=torch.uint8, device="cuda")
+        big_m[:, :301] = torch.from_numpy(marker).cuda()
+        big_k[:, :301] = torch.from_numpy(mask).cuda()
+        st = iwpp.reconstruct(big_m[:, :301], big_k[:, :301], connectivity=8, config=iwpp.Config.make(**FRONT))
+        assert st.status == 0
+        assert np.array_equal(big_m[:, :301].cpu().numpy(), ref), pitch
+        assert bool((big_m[:, 301:] == 77).all())  # the padding is not touched
+
+
+def test_front_batch_and_plan():
+    specs = synth.config3_specs(6)
+    pairs, refs, pristine = [], [], []
+    for s in specs:
+        small = synth.ImageSpec(s.index, s.width // 4, s.height // 4, s.dtype, s.conn, s.marker_kind, s.h8, s.seed)
+        marker, mask = synth.spec_images(small)
+        refs.append(oracle.reconstruct(marker, mask, s.conn))
+        tm = to_dev(marker)
+        pristine.append(tm.clone())
+        pairs.append((tm, to_dev(mask), s.conn, marker.dtype))
+    for variant in VARIANTS:
+        for p, q in zip(pairs, pristine):
+            p[0].copy_(q)
+        st = iwpp.reconstruct_batch([(p[0], p[1], p[2]) for p in pairs], variant=variant,
+                                    config=iwpp.Config.make(**FRONT))
+        assert st.status == 0
+        for p, ref in zip(pairs, refs):
+            assert np.array_equal(from_dev(p[0], p[3]), ref), variant
+    h = iwpp.Handle(0)
+    plan = iwpp.Plan(h, [(p[0], p[1], p[2]) for p in pairs], config=iwpp.Config.make(**FRONT))
+    for _ in range(2):
+        for p, q in zip(pairs, pristine):
+            p[0].copy_(q)
+        plan.launch()
+        assert plan.sync().status == 0
+        for p, ref in zip(pairs, refs):
+            assert np.array_equal(from_dev(p[0], p[3]), ref)
+    plan.close()
+    h.close()
+
+
+def test_front_timeout_is_reported():
+    # the phantom-work hook stalls the engine after the passes: the call must
+    # come back with IWPP_ERR_TIMEOUT, the result a valid lower bound
+    marker, mask = synth.config0()
+    m, k = to_dev(marker), to_dev(mask)
+    st = iwpp.reconstruct(m, k, connectivity=8, config=iwpp.Config.make(**FRONT, timeout_ms=200, phantom_work=1),
+                          check=False)
+    assert st.status == 3
+    ref = oracle.reconstruct(marker, mask, 8)
+    part = from_dev(m, marker.dtype)
+    assert np.all(part <= ref) and np.all(part >= marker)
