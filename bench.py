@@ -350,7 +350,7 @@ def bench_served(args, dev, variant):
     from iwpp import synth
 
     n_req = args.served_requests
-    times, which, specs = synth.config4_stream(n_req, 48)
+    times, which, specs = synth.config4_stream(n_req, args.served_pool)
     imgs = [synth.spec_images(s, nthreads=os.cpu_count() or 1) for s in specs]
     pin = [(_pinned(m), _pinned(k)) for m, k in imgs]
     outs = [_pinned(np.zeros_like(m)) for m, _ in imgs]
@@ -437,10 +437,11 @@ def bench_served(args, dev, variant):
     served["p99_ms_of_runs"] = [r["p99_ms"] for r in opens]
     served["bitexact"] = all(r["bitexact"] for r in opens)
     saturated = run(False)
-    return {"workload": f"{n_req} requests, Poisson 2000/s (seed 4), sides log-uniform 256..8192 "
+    return {"workload": f"{n_req} requests over {len(set(which))} distinct images, Poisson 2000/s (seed 4), "
+                        "sides log-uniform 256..8192 "
                         f"({px / n_req / 1e6:.2f} Mpx mean), uint8 80% / uint16 20%, 8-conn, "
                         "h-dome or 0.01% sparse seeds; pinned host buffers, H2D + D2H included",
-            "offered_gpx_s": px / times[-1] / 1e9, "lanes": args.lanes,
+            "offered_gpx_s": px / times[-1] / 1e9, "lanes": args.lanes, "distinct_images": len(set(which)),
             "open_loop": served, "closed_loop": saturated,
             "plain_per_request_gpx_s": px / t_plain / 1e9, "plain_bitexact": plain_ok,
             "speedup_vs_plain": saturated["gpx_s"] / (px / t_plain / 1e9),
@@ -596,7 +597,7 @@ def bench_spiral_types(args, dev, variant, handle):
                 times.append(st.device_ms)
         t = statistics.median(times) / 1e3
         res[name] = {"ms": t * 1e3, "gpx_s": W * H / t / 1e9, "hbm_frac": 3 * W * H * bpp / t / 1e9 / peak,
-                     "visits": st.visits, "tiles": st.tiles, "front_sweeps": st.front_sweeps,
+                     "visits": st.visits, "tiles": st.tiles, "top_pixels": st.top_pixels,
                      "untuned_ms": st0.device_ms,
                      "autotuned": {k_: tuned[k_] for k_ in ("tile_rows", "solver", "init_passes", "front_passes")}}
         pending.append((name, fut, _from_dev(m, marker.dtype)))
@@ -806,7 +807,7 @@ def run_ours(args):
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "bitexact": bitexact, "bitexact_timed_steps": timed_ok, "fixed_point": fixed_point_ok,
         "untuned_ms": st_untuned.device_ms,
-        "reconstruction": {"tiles": last.tiles, "visits": last.visits, "front_sweeps": last.front_sweeps,
+        "reconstruction": {"tiles": last.tiles, "visits": last.visits, "top_pixels": last.top_pixels,
                            "launches": last.launches, "corridor_pixels": n_corridor},
         "e2e": e2e,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -839,6 +840,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="only the headline line (no config1 / batched / served / spiral-type sub-results)")
     ap.add_argument("--served-requests", type=int, default=4000)
+    ap.add_argument("--served-pool", type=int, default=128,
+                    help="distinct generated image pairs the served requests draw from")
     ap.add_argument("--lanes", type=int, default=3)
     ap.add_argument("--spiral-reps", type=int, default=3)
     args = ap.parse_args()

@@ -72,11 +72,12 @@ typedef struct iwpp_config {
     int solver;                /* in-tile solver: 0 = automatic, 1 = row sweeps (fewest
                                   instructions), 2 = vertical / horizontal passes
                                   (shortest latency) */
-    int front_passes;          /* whole-image directional passes restricted to the tiles that
-                                  changed since the last pass in the same direction, repeated
-                                  until no tile changes, then the tile engine on the tiles left
-                                  unsettled: 0 = default (the tuning table's choice, else the
-                                  tile engine alone), 1 = always, 2 = never */
+    int front_passes;          /* the front stage: the pixels at the mask's largest value
+                                  raised by connected-component labelling, init_passes
+                                  whole-image passes (default 4), and the tile engine started
+                                  from the tiles still holding a pixel a neighbour can raise:
+                                  0 = default (the tuning table's choice, else the tile engine
+                                  alone), 1 = always, 2 = never */
     int phantom_work;          /* fault-injection hook for tests, 0 normally.  1: the job counts
                                   one unit of work that never arrives (a queue entry nobody
                                   inserts; for the round-based queues a CTA that never reaches
@@ -103,7 +104,7 @@ typedef struct iwpp_stats {
      * neighbour detection), queue write (state updates and insertions). */
     long long phase_cycles[5];
     long long launches;    /* kernels this library launched for the job */
-    long long front_sweeps; /* directional sweeps the front passes ran (0 without them) */
+    long long top_pixels;   /* pixels the top-level stage labelled (0 without it) */
 } iwpp_stats;
 
 /* One image of a batch. */

@@ -16,7 +16,7 @@
 
 #include "iwpp.h"
 #include "iwpp_engine.cuh"
-#include "iwpp_front.cuh"
+#include "iwpp_top.cuh"
 #include "iwpp_tune.h"
 
 using namespace iwpp;
@@ -223,9 +223,16 @@ Layout layout_for(long long n_imgs, long long G, long long cap, bool two_queues,
     return l;
 }
 
-// Sweeps the front passes may run (four per pass) before the tile engine
-// takes over whatever is left.
-constexpr int kFrontMaxSweeps = 4096;
+// Whole-image passes after the front passes when the caller leaves
+// init_passes at its default: measured on the 16384^2 spiral, four leave
+// about a tenth of the tiles to the engine.
+constexpr int kFrontFullPasses = 4;
+
+// Whole-image raster / anti-raster passes a job runs before the engine.
+int job_full_passes(const Config& c) {
+    if (c.front_passes == 1 && c.dflt_init) return kFrontFullPasses;
+    return c.init_passes;
+}
 
 long long queue_capacity_for(int variant, long long G, long long requested) {
     long long cap;
@@ -279,12 +286,12 @@ Layout job_layout(const Job& job) {
     const bool front = job.cfg.front_passes == 1;
     size_t sweep = 0;
     for (const auto& d : job.descs) {
-        if (job.cfg.init_passes > 0) {
+        if (job_full_passes(job.cfg) > 0) {
             ImgDesc dv = d;
             dv.conn = 4;
             sweep = std::max(sweep, sweep_scratch_bytes(dv));
         }
-        if (front) sweep = std::max(sweep, front_scratch_bytes(d));
+        if (front) sweep = std::max(sweep, top_scratch_bytes(d));
     }
     return layout_for((long long)job.descs.size(), job.G, job_queue_capacity(job), two, sweep, front);
 }
@@ -316,7 +323,10 @@ int build_job(Job& job, const iwpp_image* imgs, int n, int variant, const iwpp_c
             tune_lookup(tune_key(job.variant, dts.data(), cns.data(), pxs.data(), (int)dts.size()), &e)) {
             if (job.cfg.dflt_tile) job.cfg.tile_rows = e.tile_rows;
             if (job.cfg.dflt_solver) job.cfg.solver = e.solver;
-            if (job.cfg.dflt_init) job.cfg.init_passes = e.init_passes;
+            if (job.cfg.dflt_init) {
+                job.cfg.init_passes = e.init_passes;
+                job.cfg.dflt_init = false;  // the table's count stands, also with front passes
+            }
             if (job.cfg.dflt_queue && e.queue_mult > 0) job.cfg.queue_capacity = -(long long)e.queue_mult;
             if (job.cfg.dflt_front) job.cfg.front_passes = e.front_passes ? 1 : 2;
         }
@@ -624,22 +634,19 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
             ++nl;
         }
     if (front) {
-        // Front passes over each image, then the check that seeds the tile
-        // engine with the tiles still holding a pixel a neighbour can raise.
-        // The job's error word and sweep count are zeroed first: the passes
-        // write them and the engine's initialisation keeps them.
+        // The top level of each image first (its connected sets of pixels at
+        // the mask's largest value, however long); the whole-image passes and
+        // the seed check follow.  The job's error word and top-pixel count
+        // are zeroed here: the engine's initialisation keeps them.
         Ctrl* c = a.ctrl;
         e = cudaMemsetAsync(&c->error, 0, sizeof(c->error), s);
-        if (e == cudaSuccess) e = cudaMemsetAsync(&c->front_sweeps, 0, sizeof(c->front_sweeps), s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(&c->top_pixels, 0, sizeof(c->top_pixels), s);
         for (size_t i = 0; i < job.descs.size() && e == cudaSuccess; ++i)
-            e = launch_front(job.descs[i], base + l.off_sweep, &c->error, &c->front_sweeps, kFrontMaxSweeps,
-                             a.timeout_ns, device, s, &nl);
-        if (e == cudaSuccess) e = cudaMemsetAsync(seed_count, 0, sizeof(unsigned), s);
-        for (size_t i = 0; i < job.descs.size() && e == cudaSuccess; ++i)
-            e = launch_seed(job.descs[i], a.state, seed_list, seed_count, s, &nl);
+            e = launch_top(job.descs[i], base + l.off_sweep, &c->top_pixels, device, s, &nl);
         if (e != cudaSuccess) return cuda_status(e);
     }
-    for (int p = 0; p < job.cfg.init_passes; ++p)
+    const int full_passes = job_full_passes(job.cfg);
+    for (int p = 0; p < full_passes; ++p)
         for (const auto& d : job.descs)
             for (int dir = 0; dir < 4; ++dir) {
                 // raster (+X, +Y) then anti-raster (-X, -Y).  The vertical
@@ -652,6 +659,14 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
                 e = launch_sweep(dv, order[dir], s, base + l.off_sweep, &nl);
                 if (e != cudaSuccess) return cuda_status(e);
             }
+    if (front) {
+        // the tile engine starts from the tiles still holding a pixel that a
+        // neighbour can raise
+        e = cudaMemsetAsync(seed_count, 0, sizeof(unsigned), s);
+        for (size_t i = 0; i < job.descs.size() && e == cudaSuccess; ++i)
+            e = launch_seed(job.descs[i], a.state, seed_list, seed_count, s, &nl);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
     e = engine_launch_init(a, job.variant, s);
     if (e != cudaSuccess) return cuda_status(e);
     ++nl;
@@ -693,7 +708,7 @@ int read_stats(Ctrl* host_ctrl, const Workspace& ws, cudaStream_t s, long long t
         out->row_steps = (long long)host_ctrl->row_steps;
         for (int i = 0; i < 5; ++i) out->phase_cycles[i] = (long long)host_ctrl->phase[i];
         out->launches = launches;
-        out->front_sweeps = (long long)host_ctrl->front_sweeps;
+        out->top_pixels = (long long)host_ctrl->top_pixels;
     }
     return st;
 }
@@ -935,7 +950,7 @@ int iwpp_handle_sync(iwpp_handle h, iwpp_stats* stats) {
         stats->row_steps = (long long)c.row_steps;
         for (int i = 0; i < 5; ++i) stats->phase_cycles[i] = (long long)c.phase[i];
         stats->launches = h->last_launches;
-        stats->front_sweeps = (long long)c.front_sweeps;
+        stats->top_pixels = (long long)c.top_pixels;
     }
     return set_last(st);
 }
@@ -1053,7 +1068,7 @@ int iwpp_plan_sync(iwpp_plan p, iwpp_stats* stats) {
         stats->row_steps = (long long)c.row_steps;
         for (int i = 0; i < 5; ++i) stats->phase_cycles[i] = (long long)c.phase[i];
         stats->launches = p->launches;
-        stats->front_sweeps = (long long)c.front_sweeps;
+        stats->top_pixels = (long long)c.top_pixels;
     }
     return set_last(st);
 }
@@ -1223,9 +1238,13 @@ int iwpp_autotune(iwpp_handle h, const iwpp_image* images, int n, int variant, i
         // that changed, until nothing changes) before the tile engine, with
         // the best tile height and solver; long propagation paths want them
         if (best_ms >= 0.0) {
-            iwpp_config c = best;
-            c.front_passes = 1;
-            consider(c, false);
+            const iwpp_config base = best;
+            for (int ip : {2, 4, 8}) {
+                iwpp_config c = base;
+                c.front_passes = 1;
+                c.init_passes = ip;
+                consider(c, false);
+            }
         }
         // stage 3: else a fixed number of initial whole-image raster /
         // anti-raster passes, doubling while they pay (long corridors want

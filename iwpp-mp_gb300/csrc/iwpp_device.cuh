@@ -226,11 +226,11 @@ __device__ __forceinline__ void map_step_i32(uint32_t& A, uint32_t& B, int d) {
 // f(x) = max(min(x, B), A) with B = min of its mask pixels and A = its exit
 // pixel after the in-word pass; these compose associatively:
 // (A2,B2) o (A1,B1) = (max(min(A1, B2), A2), min(B1, B2)).
-template <int DT, bool FWD>
-__device__ __forceinline__ void hscan(uint32_t (&m)[Px<DT>::PPW], const uint32_t (&k)[Px<DT>::PPW], uint32_t cin,
-                                      int lane) {
+// N: pixels per lane (one 32-bit word by default; the 16-byte-lane sweeps
+// hold four words).
+template <int DT, bool FWD, int N = Px<DT>::PPW>
+__device__ __forceinline__ void hscan(uint32_t (&m)[N], const uint32_t (&k)[N], uint32_t cin, int lane) {
     using P = Px<DT>;
-    constexpr int N = P::PPW;
 #pragma unroll
     for (int s = 1; s < N; ++s) {
         const int j = FWD ? s : N - 1 - s;

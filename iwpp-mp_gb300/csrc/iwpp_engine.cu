@@ -695,7 +695,7 @@ __global__ void engine_init_kernel(EngineArgs a, int variant) {
         c->pushes = 0ull;
         c->row_steps = 0ull;
         for (int i = 0; i < 5; ++i) c->phase[i] = 0ull;
-        if (!a.front) c->front_sweeps = 0ull;  // else the front passes' count stands
+        if (!a.front) c->top_pixels = 0ull;  // else the top-level stage's count stands
     }
 }
 

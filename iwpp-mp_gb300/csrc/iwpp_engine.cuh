@@ -65,7 +65,7 @@ struct Ctrl {
     unsigned long long pushes;
     unsigned long long row_steps;
     unsigned long long phase[5];  // cycles: queue read, fetch, processing, dump, queue write
-    unsigned long long front_sweeps;  // directional sweeps run by the front passes
+    unsigned long long top_pixels;    // pixels the top-level stage labelled
     unsigned ninit;     // initial entries (every tile, or the seed list after front passes)
 };
 

@@ -150,6 +150,99 @@ __global__ void sweep_x_kernel(ImgDesc d) {
     }
 }
 
+// The same sweep with 16-byte lanes (a warp chunk is 512 bytes): the lane's
+// four words are scanned in registers and the warp's clamp-map composition
+// runs once per 16 bytes instead of once per 4, which is what the 4-byte form
+// spends its issue slots on.  Rows must start on 16-byte boundaries (base
+// and pitch of both planes); the row's last partial lane is loaded and
+// stored word by word.
+template <int DT, bool FWD>
+__global__ void sweep_x16_kernel(ImgDesc d) {
+    using P = Px<DT>;
+    constexpr int WPL = 4;             // words per lane
+    constexpr int N = WPL * P::PPW;    // pixels per lane
+    constexpr int CW = 32 * N;         // pixels per chunk
+    const int lane = threadIdx.x & 31;
+    const int row = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (row >= d.H) return;
+    const int chunks = (d.W + CW - 1) / CW;
+    unsigned char* mbase = d.marker + (size_t)row * d.pitch_m;
+    const unsigned char* kbase = d.mask + (size_t)row * d.pitch_k;
+    auto px0_of = [&](int cc) { return (FWD ? cc : chunks - 1 - cc) * CW + lane * N; };
+    auto fetch = [&](int cc, uint4& mv, uint4& kv) {
+        mv = make_uint4(P::MINW, P::MINW, P::MINW, P::MINW);
+        kv = mv;
+        if (cc >= chunks) return;
+        const int px0 = px0_of(cc), npx = d.W - px0;
+        if (npx >= N) {
+            mv = __ldcg(reinterpret_cast<const uint4*>(mbase + (size_t)px0 * P::BPP));
+            kv = __ldg(reinterpret_cast<const uint4*>(kbase + (size_t)px0 * P::BPP));
+        } else if (npx > 0) {
+            uint32_t mw[WPL], kw[WPL];
+#pragma unroll
+            for (int w = 0; w < WPL; ++w) {
+                const int n = npx - w * P::PPW;
+                mw[w] = P::MINW;
+                kw[w] = P::MINW;
+                if (n > 0)
+                    load_pair<DT>(mbase + (size_t)(px0 + w * P::PPW) * P::BPP,
+                                  kbase + (size_t)(px0 + w * P::PPW) * P::BPP, n, mw[w], kw[w]);
+            }
+            mv = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+            kv = make_uint4(kw[0], kw[1], kw[2], kw[3]);
+        }
+    };
+    uint4 mq[kXAhead], kq[kXAhead];
+#pragma unroll
+    for (int q = 0; q < kXAhead; ++q) fetch(q, mq[q], kq[q]);
+    uint32_t carry = P::MINPX;
+    for (int c0 = 0; c0 < chunks; c0 += kXAhead) {
+#pragma unroll
+        for (int q = 0; q < kXAhead; ++q) {
+            const int cc = c0 + q;
+            if (cc >= chunks) break;  // warp-uniform
+            const uint4 mv = mq[q], kv = kq[q];
+            fetch(cc + kXAhead, mq[q], kq[q]);
+            const uint32_t mw[WPL] = {mv.x, mv.y, mv.z, mv.w}, kw[WPL] = {kv.x, kv.y, kv.z, kv.w};
+            uint32_t m[N], k[N];
+#pragma unroll
+            for (int w = 0; w < WPL; ++w) {
+                uint32_t a[P::PPW], b[P::PPW];
+                P::unpack(mw[w], a);
+                P::unpack(kw[w], b);
+#pragma unroll
+                for (int j = 0; j < P::PPW; ++j) {
+                    m[w * P::PPW + j] = a[j];
+                    k[w * P::PPW + j] = b[j];
+                }
+            }
+            hscan<DT, FWD, N>(m, k, carry, lane);
+            uint32_t nw[WPL];
+            bool chg = false;
+#pragma unroll
+            for (int w = 0; w < WPL; ++w) {
+                uint32_t a[P::PPW];
+#pragma unroll
+                for (int j = 0; j < P::PPW; ++j) a[j] = m[w * P::PPW + j];
+                nw[w] = P::pack(a);
+                chg |= nw[w] != mw[w];
+            }
+            const int px0 = px0_of(cc), npx = d.W - px0;
+            if (chg && npx > 0) {
+                unsigned char* dst = mbase + (size_t)px0 * P::BPP;
+                if (npx >= N) {
+                    *reinterpret_cast<uint4*>(dst) = make_uint4(nw[0], nw[1], nw[2], nw[3]);
+                } else {
+#pragma unroll
+                    for (int w = 0; w < WPL; ++w)
+                        if (npx - w * P::PPW > 0) store_word_plain<DT>(dst + w * 4, npx - w * P::PPW, nw[w]);
+                }
+            }
+            carry = FWD ? __shfl_sync(FULL, m[N - 1], 31) : __shfl_sync(FULL, m[0], 0);
+        }
+    }
+}
+
 // --------------------------------------------------------------- Y sweeps
 // 4-byte asynchronous global -> shared copy (cp.async, LDGSTS) and its
 // group bookkeeping.
@@ -566,10 +659,19 @@ static int launch_sweep_t(const ImgDesc& d, int direction, cudaStream_t s, void*
     constexpr int TW = 32 * P::PPW;
     if (direction == 0 || direction == 2) {
         const unsigned blocks = blocks_for((long long)d.H * 32, 128);
-        if (direction == 0)
+        const bool aligned16 =
+            ((reinterpret_cast<uintptr_t>(d.marker) | reinterpret_cast<uintptr_t>(d.mask)) & 15u) == 0u &&
+            ((d.pitch_m | d.pitch_k) & 15) == 0;
+        if (aligned16) {
+            if (direction == 0)
+                sweep_x16_kernel<DT, true><<<blocks, 128, 0, s>>>(d);
+            else
+                sweep_x16_kernel<DT, false><<<blocks, 128, 0, s>>>(d);
+        } else if (direction == 0) {
             sweep_x_kernel<DT, true><<<blocks, 128, 0, s>>>(d);
-        else
+        } else {
             sweep_x_kernel<DT, false><<<blocks, 128, 0, s>>>(d);
+        }
         return 1;
     } else {
         const int strips = (d.W + TW - 1) / TW;

@@ -1,0 +1,698 @@
+// iwpp_top.cu -- the front stage: reconstruction of the image's highest level
+// set by connected-component labelling; and the check that seeds the tile
+// engine with the tiles still violating a constraint after the whole-image
+// passes.
+//
+// Only pixels whose mask is at the image's largest value T can rise in this
+// stage; each rises to the largest marker (capped at T) of the connected set
+// of such pixels it belongs to (the image's connectivity).  This is the
+// reconstruction restricted to that level set, so it never exceeds the full
+// reconstruction (every member of a component reaches every other through
+// pixels whose mask is T): a valid start for the whole-image passes and the
+// tile engine that follow.  The rule is the reference's
+// (IWPP MP/src/MorphologicalReconstruction.cu:43-44) applied to closure.
+//
+// Why: a long path at the top level (a one-pixel corridor spiralling through
+// the image) needs one directional sweep per straight run, or one dependent
+// tile visit per tile it crosses; labelling finds its component in a fixed
+// number of passes over the tiles that hold top-level pixels:
+//   1. top_max_kernel: every tile's largest mask value (as an unsigned key)
+//      and the image's (T).
+//   2. top_local_kernel (one CTA per tile holding T): the tile's top-level
+//      pixels compacted into a list, union-find over them in shared memory;
+//      each local component gets one of kTopSlots node slots (rootidx: its
+//      least pixel index, the root union-by-least-index leaves), its largest
+//      capped marker (gmax) and the slots of the tile's edge pixels (edge).
+//      A tile with more components than slots leaves the extra ones out
+//      (they only keep their own values: still valid).
+//   3. top_union_kernel: union of the nodes of top-level pixels that touch
+//      across tile edges (and corners with 8-connectivity), a lock-free
+//      global union-find (link the larger root under the smaller).
+//   4. top_flatten_kernel: every node to its root; each root's gmax the
+//      largest of its component.
+//   5. top_apply_kernel: the local labelling again (the roots are the least
+//      pixel indices, so it is the same), each top-level pixel raised to its
+//      component's value.
+#include "iwpp_engine.cuh"
+#include "iwpp_top.cuh"
+
+namespace iwpp {
+
+constexpr int kTopRows = 64;    // rows of a tile (tiles are 128 bytes wide)
+constexpr int kTopSlots = 64;   // component nodes one tile can export
+constexpr int kTopThreads = 256;
+
+// Order-preserving unsigned key of a pixel value (int32 with its sign bit
+// flipped), and back.
+template <int DT>
+__device__ __forceinline__ uint32_t top_key(uint32_t v) { return DT == DT_I32 ? v ^ 0x80000000u : v; }
+
+struct TopArgs {
+    ImgDesc d;
+    int tx_n, ty_n, tw;      // tiles across, down; pixels per tile row
+    int conn;
+    unsigned* tmax;          // per tile: largest mask key
+    unsigned* thr_key;       // the image's largest mask key
+    int* ns;                 // per tile: node slots used
+    int* gparent;            // per node (tile * kTopSlots + slot): parent node
+    unsigned* gmax;          // per node: largest capped marker key of its component
+    unsigned short* rootidx; // per node: the component's least pixel index in its tile
+    signed char* edge;       // per tile: left (64), right (64), top (tw), bottom (tw) slot or -1
+    int edge_stride;         // 128 + 2 * tw
+    unsigned long long* top_pixels;  // the job's count of pixels labelled
+};
+
+__device__ __forceinline__ int g_find(int* parent, int x) {
+    for (;;) {
+        const int p = __ldcg(&parent[x]);
+        if (p == x) return x;
+        const int gp = __ldcg(&parent[p]);
+        if (gp != p) atomicCAS(&parent[x], p, gp);  // path halving
+        x = gp;
+    }
+}
+
+__device__ __forceinline__ void g_union(int* parent, int a, int b) {
+    for (;;) {
+        a = g_find(parent, a);
+        b = g_find(parent, b);
+        if (a == b) return;
+        if (a < b) {
+            const int t = a;
+            a = b;
+            b = t;
+        }
+        // link the larger root under the smaller
+        const int old = atomicCAS(&parent[a], a, b);
+        if (old == a) return;
+        a = old;
+    }
+}
+
+__device__ __forceinline__ int s_find(int* parent, int x) {
+    for (;;) {
+        const int p = *(volatile int*)&parent[x];
+        if (p == x) return x;
+        x = p;
+    }
+}
+
+__device__ __forceinline__ void s_union(int* parent, int a, int b) {
+    for (;;) {
+        a = s_find(parent, a);
+        b = s_find(parent, b);
+        if (a == b) return;
+        if (a < b) {
+            const int t = a;
+            a = b;
+            b = t;
+        }
+        const int old = atomicCAS(&parent[a], a, b);
+        if (old == a) return;
+        a = old;
+    }
+}
+
+// ------------------------------------------------------------ 1. maxima
+template <int DT>
+__global__ void top_max_kernel(TopArgs a) {
+    using P = Px<DT>;
+    const int lane = threadIdx.x & 31;
+    const long long G = (long long)a.tx_n * a.ty_n;
+    const long long wg = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    const ImgDesc& d = a.d;
+    const long long row_bytes = (long long)d.W * P::BPP;
+    for (long long t = wg; t < G; t += nw) {
+        const int ty = (int)(t / a.tx_n), tx = (int)(t - (long long)ty * a.tx_n);
+        const int y0 = ty * kTopRows, rows = min(kTopRows, d.H - y0);
+        const long long byte0 = (long long)tx * 128 + lane * 4;
+        const int npx = byte0 < row_bytes ? (int)min((long long)P::PPW, (row_bytes - byte0) / P::BPP) : 0;
+        uint32_t best = 0u;  // keys: 0 is at or below every pixel
+        if (npx > 0)
+            for (int r = 0; r < rows; ++r) {
+                const uint32_t kw = load_word_plain<DT>(d.mask + (size_t)(y0 + r) * d.pitch_k + byte0, npx, false);
+                uint32_t k[P::PPW];
+                P::unpack(kw, k);
+#pragma unroll
+                for (int j = 0; j < P::PPW; ++j)
+                    if (j < npx) best = max(best, top_key<DT>(k[j]));
+            }
+        best = __reduce_max_sync(FULL, best);
+        if (lane == 0) {
+            a.tmax[t] = best;
+            atomicMax(a.thr_key, best);
+        }
+    }
+}
+
+// ------------------------------------------------- 2 / 5. local labelling
+// Shared memory of a CTA working on one tile: the union-find parents of the
+// tile's pixels (-1: not at the top level), the list of its top-level
+// pixels, the node slot of each root and per slot its component's value.
+template <int DT>
+struct TopSmem {
+    static constexpr int NPX = kTopRows * 32 * Px<DT>::PPW;
+    int parent[NPX];
+    unsigned short list[NPX];
+    signed char slot[NPX];
+    unsigned sval[kTopSlots];  // local: largest capped marker key; apply: the component's
+    int warp_count[kTopThreads / 32];
+    int nlist;
+    int nslots;
+};
+
+// Lane words a thread of the labelling CTA covers: word w = threadIdx.x +
+// i * kTopThreads is tile row w / 32, lane word w % 32.
+constexpr int kTopWpt = kTopRows * 32 / kTopThreads;
+
+// The tile's top-level pixels labelled: sm.list[0, sm.nlist) holds them,
+// sm.parent[p] the least pixel index of p's component (-1 for the other
+// pixels).  Returns the thread's top-level flags: bit i * PPW + j for pixel j
+// of its word i.  All threads of the CTA.
+template <int DT>
+__device__ unsigned label_tile(const TopArgs& a, int tx, int ty, unsigned tkey, TopSmem<DT>& sm) {
+    using P = Px<DT>;
+    constexpr int TW = 32 * P::PPW;
+    const ImgDesc& d = a.d;
+    const int x0 = tx * TW, y0 = ty * kTopRows;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // the tile's mask one lane word at a time, all of a thread's words in
+    // flight together
+    uint32_t kw[kTopWpt];
+#pragma unroll
+    for (int i = 0; i < kTopWpt; ++i) {
+        const int w = threadIdx.x + i * kTopThreads;
+        const int y = y0 + (w >> 5), px0 = x0 + (w & 31) * P::PPW;
+        kw[i] = y < d.H && px0 < d.W
+                    ? load_word_plain<DT>(d.mask + (size_t)y * d.pitch_k + (size_t)px0 * P::BPP, d.W - px0, false)
+                    : P::MINW;
+    }
+    unsigned bits = 0u;
+#pragma unroll
+    for (int i = 0; i < kTopWpt; ++i) {
+        const int w = threadIdx.x + i * kTopThreads;
+        const int r = w >> 5, c0 = (w & 31) * P::PPW;
+        uint32_t k[P::PPW];
+        P::unpack(kw[i], k);
+#pragma unroll
+        for (int j = 0; j < P::PPW; ++j) {
+            const int p = r * TW + c0 + j;
+            const bool top = y0 + r < d.H && x0 + c0 + j < d.W && top_key<DT>(k[j]) >= tkey;
+            sm.parent[p] = top ? p : -1;
+            if (top) bits |= 1u << (i * P::PPW + j);
+        }
+    }
+    // the list: each thread's place by a CTA-wide exclusive scan of counts
+    const int cnt = __popc(bits);
+    int incl = cnt;
+#pragma unroll
+    for (int dd = 1; dd < 32; dd <<= 1) {
+        const int v = __shfl_up_sync(FULL, incl, dd);
+        if (lane >= dd) incl += v;
+    }
+    if (lane == 31) sm.warp_count[warp] = incl;
+    __syncthreads();
+    int pos = incl - cnt;
+    for (int q = 0; q < warp; ++q) pos += sm.warp_count[q];
+    if (threadIdx.x == kTopThreads - 1) sm.nlist = pos + cnt;
+    for (unsigned b = bits; b; b &= b - 1u) {
+        const int bit = __ffs(b) - 1;
+        const int i = bit / P::PPW, j = bit - i * P::PPW;
+        const int w = threadIdx.x + i * kTopThreads;
+        sm.list[pos++] = (unsigned short)((w >> 5) * TW + (w & 31) * P::PPW + j);
+    }
+    __syncthreads();
+    const int n = sm.nlist;
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int p = sm.list[e];
+        const int r = p / TW, c = p - r * TW;
+        if (c > 0 && sm.parent[p - 1] >= 0) s_union(sm.parent, p, p - 1);
+        if (r > 0) {
+            if (sm.parent[p - TW] >= 0) s_union(sm.parent, p, p - TW);
+            if (a.conn == 8) {
+                if (c > 0 && sm.parent[p - TW - 1] >= 0) s_union(sm.parent, p, p - TW - 1);
+                if (c + 1 < TW && sm.parent[p - TW + 1] >= 0) s_union(sm.parent, p, p - TW + 1);
+            }
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int p = sm.list[e];
+        sm.parent[p] = s_find(sm.parent, p);
+    }
+    __syncthreads();
+    return bits;
+}
+
+// The thread's marker words that hold a top-level pixel (per `bits`), all in
+// flight together; the others are left 0.
+template <int DT>
+__device__ __forceinline__ void load_top_words(const ImgDesc& d, int tx, int ty, unsigned bits,
+                                               uint32_t (&mw)[kTopWpt]) {
+    using P = Px<DT>;
+    constexpr int TW = 32 * P::PPW;
+    constexpr unsigned WMASK = (1u << P::PPW) - 1u;
+#pragma unroll
+    for (int i = 0; i < kTopWpt; ++i) {
+        const int w = threadIdx.x + i * kTopThreads;
+        const int y = ty * kTopRows + (w >> 5), px0 = tx * TW + (w & 31) * P::PPW;
+        mw[i] = (bits >> (i * P::PPW)) & WMASK
+                    ? load_word_plain<DT>(d.marker + (size_t)y * d.pitch_m + (size_t)px0 * P::BPP, d.W - px0, true)
+                    : 0u;
+    }
+}
+
+template <int DT>
+__global__ void __launch_bounds__(kTopThreads) top_local_kernel(TopArgs a) {
+    using P = Px<DT>;
+    constexpr int TW = 32 * P::PPW;
+    extern __shared__ __align__(16) unsigned char top_smem[];
+    TopSmem<DT>& sm = *reinterpret_cast<TopSmem<DT>*>(top_smem);
+    const ImgDesc& d = a.d;
+    const unsigned tkey = *(const volatile unsigned*)a.thr_key;
+    const uint32_t tval = top_key<DT>(tkey);
+    const long long G = (long long)a.tx_n * a.ty_n;
+    for (long long t = blockIdx.x; t < G; t += gridDim.x) {
+        if (a.tmax[t] < tkey) continue;  // no top-level pixel (CTA-uniform)
+        const int ty = (int)(t / a.tx_n), tx = (int)(t - (long long)ty * a.tx_n);
+        if (threadIdx.x == 0) sm.nslots = 0;
+        const unsigned bits = label_tile<DT>(a, tx, ty, tkey, sm);
+        const int n = sm.nlist;
+        // the marker words with top-level pixels in flight while the roots
+        // take their node slots
+        uint32_t mw[kTopWpt];
+        load_top_words<DT>(d, tx, ty, bits, mw);
+        for (int e = threadIdx.x; e < n; e += blockDim.x) {
+            const int p = sm.list[e];
+            if (sm.parent[p] != p) continue;
+            const int s = atomicAdd(&sm.nslots, 1);
+            sm.slot[p] = s < kTopSlots ? (signed char)s : (signed char)-1;
+            if (s < kTopSlots) {
+                const long long node = t * kTopSlots + s;
+                a.rootidx[node] = (unsigned short)p;
+                a.gparent[node] = (int)node;
+                sm.sval[s] = 0u;
+            }
+        }
+        __syncthreads();
+        // each component's largest marker capped at the level (its mask): a
+        // thread's pixels run by component, one shared atomic per run
+        constexpr unsigned WMASK = (1u << P::PPW) - 1u;
+        int cur = -1;
+        unsigned best = 0u;
+#pragma unroll
+        for (int i = 0; i < kTopWpt; ++i) {
+            const unsigned wb = (bits >> (i * P::PPW)) & WMASK;
+            if (!wb) continue;
+            const int w = threadIdx.x + i * kTopThreads;
+            const int pbase = (w >> 5) * TW + (w & 31) * P::PPW;
+            uint32_t m[P::PPW];
+            P::unpack(mw[i], m);
+#pragma unroll
+            for (int j = 0; j < P::PPW; ++j) {
+                if (!((wb >> j) & 1u)) continue;
+                const int s = sm.slot[sm.parent[pbase + j]];
+                if (s < 0) continue;
+                const unsigned v = top_key<DT>(P::mn(m[j], tval));
+                if (s != cur) {
+                    if (cur >= 0) atomicMax(&sm.sval[cur], best);
+                    cur = s;
+                    best = v;
+                } else {
+                    best = max(best, v);
+                }
+            }
+        }
+        if (cur >= 0) atomicMax(&sm.sval[cur], best);
+        // the slots of the edge pixels: left and right columns, top and
+        // bottom rows (-1: not at the top level, or a component left out)
+        signed char* e = a.edge + t * a.edge_stride;
+        for (int i = threadIdx.x; i < 128 + 2 * TW; i += blockDim.x) {
+            int p;
+            if (i < 64) p = i * TW;                          // left column, row i
+            else if (i < 128) p = (i - 64) * TW + TW - 1;    // right column
+            else if (i < 128 + TW) p = i - 128;              // top row
+            else p = (kTopRows - 1) * TW + (i - 128 - TW);   // bottom row
+            const int root = sm.parent[p];
+            e[i] = root < 0 ? (signed char)-1 : sm.slot[root];
+        }
+        __syncthreads();
+        const int ns = min(sm.nslots, kTopSlots);
+        for (int q = threadIdx.x; q < ns; q += blockDim.x) a.gmax[t * kTopSlots + q] = sm.sval[q];
+        if (threadIdx.x == 0) {
+            a.ns[t] = ns;
+            atomicAdd(a.top_pixels, (unsigned long long)n);
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------ 3. edge unions
+// One thread per edge pixel pair of a tile and its right / lower neighbour
+// (and the corners for 8-connectivity); both tiles must hold top-level
+// pixels (their edge slots are written).
+__global__ void top_union_kernel(TopArgs a) {
+    const int TW = a.tw;
+    const long long G = (long long)a.tx_n * a.ty_n;
+    const int per = 2 * kTopRows + 2 * TW + 2;  // work items per tile
+    const unsigned tkey = *(const volatile unsigned*)a.thr_key;
+    const long long total = G * per;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long t = i / per;
+        const int k = (int)(i - t * per);
+        if (a.tmax[t] < tkey) continue;
+        const int ty = (int)(t / a.tx_n), tx = (int)(t - (long long)ty * a.tx_n);
+        const signed char* e = a.edge + t * a.edge_stride;
+        auto node = [&](long long tile, int s) { return (int)(tile * kTopSlots + s); };
+        auto link = [&](int sa, long long tb, int sb) {
+            if (sa >= 0 && sb >= 0) g_union(a.gparent, node(t, sa), node(tb, sb));
+        };
+        if (k < 2 * kTopRows) {
+            // right neighbour: this tile's right column against its left column
+            if (tx + 1 >= a.tx_n) continue;
+            const long long tb = t + 1;
+            if (a.tmax[tb] < tkey) continue;
+            const signed char* eb = a.edge + tb * a.edge_stride;
+            const int r = k >> 1;
+            const int sa = e[64 + r];
+            if (sa < 0) continue;
+            if ((k & 1) == 0) {
+                link(sa, tb, eb[r]);
+            } else if (a.conn == 8) {
+                if (r > 0) link(sa, tb, eb[r - 1]);
+                if (r + 1 < kTopRows) link(sa, tb, eb[r + 1]);
+            }
+        } else if (k < 2 * kTopRows + 2 * TW) {
+            // lower neighbour: this tile's bottom row against its top row
+            if (ty + 1 >= a.ty_n) continue;
+            const long long tb = t + a.tx_n;
+            if (a.tmax[tb] < tkey) continue;
+            const signed char* eb = a.edge + tb * a.edge_stride;
+            const int j = k - 2 * kTopRows;
+            const int c = j >> 1;
+            const int sa = e[128 + TW + c];
+            if (sa < 0) continue;
+            if ((j & 1) == 0) {
+                link(sa, tb, eb[128 + c]);
+            } else if (a.conn == 8) {
+                if (c > 0) link(sa, tb, eb[128 + c - 1]);
+                if (c + 1 < TW) link(sa, tb, eb[128 + c + 1]);
+            }
+        } else if (a.conn == 8 && ty + 1 < a.ty_n) {
+            // corners: bottom-right pixel to the lower-right tile's top-left,
+            // bottom-left pixel to the lower-left tile's top-right
+            if (k == 2 * kTopRows + 2 * TW) {
+                if (tx + 1 >= a.tx_n) continue;
+                const long long tb = t + a.tx_n + 1;
+                if (a.tmax[tb] < tkey) continue;
+                link(e[128 + TW + TW - 1], tb, a.edge[tb * a.edge_stride + 128]);
+            } else {
+                if (tx == 0) continue;
+                const long long tb = t + a.tx_n - 1;
+                if (a.tmax[tb] < tkey) continue;
+                link(e[128 + TW], tb, a.edge[tb * a.edge_stride + 128 + TW - 1]);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------- 4. flatten
+__global__ void top_flatten_kernel(TopArgs a) {
+    const long long total = (long long)a.tx_n * a.ty_n * kTopSlots;
+    const unsigned tkey = *(const volatile unsigned*)a.thr_key;
+    for (long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x; node < total;
+         node += (long long)gridDim.x * blockDim.x) {
+        const long long t = node / kTopSlots;
+        const int s = (int)(node - t * kTopSlots);
+        if (a.tmax[t] < tkey || s >= a.ns[t]) continue;
+        const int root = g_find(a.gparent, (int)node);
+        a.gparent[node] = root;
+        if (root != (int)node) atomicMax(&a.gmax[root], __ldcg(&a.gmax[node]));
+    }
+}
+
+// ------------------------------------------------------------ 5. apply
+template <int DT>
+__global__ void __launch_bounds__(kTopThreads) top_apply_kernel(TopArgs a) {
+    using P = Px<DT>;
+    constexpr int TW = 32 * P::PPW;
+    extern __shared__ __align__(16) unsigned char top_smem[];
+    TopSmem<DT>& sm = *reinterpret_cast<TopSmem<DT>*>(top_smem);
+    const ImgDesc& d = a.d;
+    const unsigned tkey = *(const volatile unsigned*)a.thr_key;
+    const long long G = (long long)a.tx_n * a.ty_n;
+    for (long long t = blockIdx.x; t < G; t += gridDim.x) {
+        if (a.tmax[t] < tkey) continue;
+        const int ty = (int)(t / a.tx_n), tx = (int)(t - (long long)ty * a.tx_n);
+        const unsigned bits = label_tile<DT>(a, tx, ty, tkey, sm);
+        const int n = sm.nlist;
+        uint32_t mw[kTopWpt];
+        load_top_words<DT>(d, tx, ty, bits, mw);
+        // the slot of each root, from the node table's least pixel indices,
+        // and each slot's component value, read once
+        const int ns = a.ns[t];
+        for (int e = threadIdx.x; e < n; e += blockDim.x) {
+            const int p = sm.list[e];
+            if (sm.parent[p] != p) continue;
+            signed char s = -1;
+            for (int q = 0; q < ns; ++q)
+                if (a.rootidx[t * kTopSlots + q] == (unsigned short)p) s = (signed char)q;
+            sm.slot[p] = s;
+        }
+        for (int q = threadIdx.x; q < ns; q += blockDim.x)
+            sm.sval[q] = __ldcg(&a.gmax[g_find(a.gparent, (int)(t * kTopSlots + q))]);
+        __syncthreads();
+        // the words with a top-level pixel raised and written back
+        constexpr unsigned WMASK = (1u << P::PPW) - 1u;
+#pragma unroll
+        for (int i = 0; i < kTopWpt; ++i) {
+            const unsigned wb = (bits >> (i * P::PPW)) & WMASK;
+            if (!wb) continue;
+            const int w = threadIdx.x + i * kTopThreads;
+            const int pbase = (w >> 5) * TW + (w & 31) * P::PPW;
+            uint32_t m[P::PPW];
+            P::unpack(mw[i], m);
+            bool chg = false;
+#pragma unroll
+            for (int j = 0; j < P::PPW; ++j) {
+                if (!((wb >> j) & 1u)) continue;
+                const int s = sm.slot[sm.parent[pbase + j]];
+                if (s < 0) continue;
+                const uint32_t v = top_key<DT>(sm.sval[s]);
+                if (P::gt(v, m[j])) {
+                    m[j] = v;
+                    chg = true;
+                }
+            }
+            if (!chg) continue;
+            const int y = ty * kTopRows + (w >> 5), px0 = tx * TW + (w & 31) * P::PPW;
+            unsigned char* row = d.marker + (size_t)y * d.pitch_m + (size_t)px0 * P::BPP;
+            const int npx = d.W - px0;
+            if (npx >= P::PPW) {
+                *reinterpret_cast<unsigned int*>(row) = P::pack(m);
+            } else {
+#pragma unroll
+                for (int j = 0; j < P::PPW; ++j)
+                    if (j < npx) P::st_px(row + j * P::BPP, m[j]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// --------------------------------------------------------- engine seeding
+// After the front stage and the whole-image passes the tile engine must
+// still visit every tile holding a pixel that a neighbour could raise (with
+// 8-connectivity: across the diagonals too).  One warp per engine tile (TH
+// rows, 128 bytes wide) streams the tile's rows with the rows above and
+// below, one word per lane, neighbours across lanes by shuffles and across
+// tiles by the halo columns (lanes 0 / 31); it marks a tile with such a
+// pixel DIRTY on all sides and appends it to the seed list; other tiles get
+// state 0.
+template <int DT>
+__device__ __forceinline__ uint32_t seed_word(const ImgDesc& d, const unsigned char* base, long long pitch, int y,
+                                              int px0) {
+    using P = Px<DT>;
+    if (y < 0 || y >= d.H || px0 >= d.W) return P::MINW;
+    return load_word_plain<DT>(base + (size_t)y * pitch + (size_t)px0 * P::BPP, d.W - px0, false);
+}
+
+template <int DT>
+__device__ __forceinline__ uint32_t seed_px(const ImgDesc& d, int y, int x) {
+    using P = Px<DT>;
+    if (y < 0 || y >= d.H || x < 0 || x >= d.W) return P::MINPX;
+    return P::ld_px(d.marker + (size_t)y * d.pitch_m + (size_t)x * P::BPP);
+}
+
+template <int DT>
+__global__ void seed_kernel(const ImgDesc d, unsigned* state, unsigned* list, unsigned* nlist) {
+    using P = Px<DT>;
+    constexpr int N = P::PPW;
+    constexpr int TW = 32 * N;
+    const int lane = threadIdx.x & 31;
+    const long long tiles = (long long)d.tiles_x * d.tiles_y;
+    const long long wg = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int TH = d.tile_rows;
+    for (long long t = wg; t < tiles; t += nw) {
+        const int ty = (int)(t / d.tiles_x), tx = (int)(t - (long long)ty * d.tiles_x);
+        const int x0 = tx * TW, y0 = ty * TH, rows = min(TH, d.H - y0);
+        const int px0 = x0 + lane * N;
+        // marker words of rows y - 1, y, y + 1 (rolling), and for lanes 0 / 31
+        // the halo column pixel beside the tile in the same three rows
+        uint32_t wu = seed_word<DT>(d, d.marker, d.pitch_m, y0 - 1, px0);
+        uint32_t wc = seed_word<DT>(d, d.marker, d.pitch_m, y0, px0);
+        const int hx = lane == 0 ? x0 - 1 : x0 + TW;
+        uint32_t hu = seed_px<DT>(d, y0 - 1, hx), hc = seed_px<DT>(d, y0, hx);
+        bool bad = false;
+        for (int r = 0; r < rows; ++r) {
+            const int y = y0 + r;
+            const uint32_t wd = seed_word<DT>(d, d.marker, d.pitch_m, y + 1, px0);
+            const uint32_t wk = seed_word<DT>(d, d.mask, d.pitch_k, y, px0);
+            const uint32_t hd = seed_px<DT>(d, y + 1, hx);
+            uint32_t u[N], c[N], dn[N], k[N];
+            P::unpack(wu, u);
+            P::unpack(wc, c);
+            P::unpack(wd, dn);
+            P::unpack(wk, k);
+            // per column: the larger of the pixels above and below (the
+            // vertical neighbours) and the largest of all three (what a
+            // column offers its side neighbours with 8-connectivity)
+            uint32_t v2[N], v3[N];
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+                v2[j] = P::mx(u[j], dn[j]);
+                v3[j] = P::mx(v2[j], c[j]);
+            }
+            // the columns left of the lane's first pixel and right of its last
+            const uint32_t side_l = d.conn == 8 ? v3[N - 1] : c[N - 1];
+            const uint32_t side_r = d.conn == 8 ? v3[0] : c[0];
+            uint32_t left = __shfl_up_sync(FULL, side_l, 1), right = __shfl_down_sync(FULL, side_r, 1);
+            const uint32_t halo = d.conn == 8 ? P::mx(P::mx(hu, hc), hd) : hc;
+            if (lane == 0) left = halo;
+            if (lane == 31) right = halo;
+            bool mine = false;
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+                const uint32_t l = j == 0 ? left : (d.conn == 8 ? v3[j - 1] : c[j - 1]);
+                const uint32_t rr = j == N - 1 ? right : (d.conn == 8 ? v3[j + 1] : c[j + 1]);
+                const uint32_t best = P::mx(v2[j], P::mx(l, rr));
+                mine |= P::gt(P::mn(best, k[j]), c[j]) && px0 + j < d.W;
+            }
+            if (__any_sync(FULL, mine)) {
+                bad = true;
+                break;
+            }
+            wu = wc;
+            wc = wd;
+            hu = hc;
+            hc = hd;
+        }
+        const unsigned g = (unsigned)d.tile_base + (unsigned)t;
+        if (lane == 0) {
+            state[g] = bad ? (ST_DIRTY | ST_SIDES) : 0u;
+            if (bad) list[atomicAdd(nlist, 1u)] = g;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ host
+static size_t tal(size_t v) { return (v + 255) / 256 * 256; }
+
+static void top_dims(const ImgDesc& d, int* tx_n, int* ty_n, int* tw) {
+    const int bpp = d.dtype == DT_U8 ? 1 : d.dtype == DT_U16 ? 2 : 4;
+    *tw = 128 / bpp;
+    *tx_n = (int)(((long long)d.W * bpp + 127) / 128);
+    *ty_n = (d.H + kTopRows - 1) / kTopRows;
+}
+
+size_t top_scratch_bytes(const ImgDesc& d) {
+    int tx_n, ty_n, tw;
+    top_dims(d, &tx_n, &ty_n, &tw);
+    const size_t G = (size_t)tx_n * ty_n, nodes = G * kTopSlots;
+    return tal(256) + tal(G * 4) + tal(G * 4) + tal(nodes * 4) + tal(nodes * 4) + tal(nodes * 2) +
+           tal(G * (128 + 2 * (size_t)tw));
+}
+
+template <int DT>
+static cudaError_t launch_top_t(const TopArgs& a, int sms, cudaStream_t s) {
+    const size_t smem = sizeof(TopSmem<DT>);
+    cudaError_t e = cudaFuncSetAttribute(top_local_kernel<DT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(top_apply_kernel<DT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const long long G = (long long)a.tx_n * a.ty_n;
+    long long wblocks = (G * 32 + 255) / 256;
+    if (wblocks > (long long)sms * 16) wblocks = (long long)sms * 16;
+    top_max_kernel<DT><<<(unsigned)wblocks, 256, 0, s>>>(a);
+    long long cblocks = G < (long long)sms * 4 ? G : (long long)sms * 4;
+    top_local_kernel<DT><<<(unsigned)cblocks, kTopThreads, smem, s>>>(a);
+    const long long upairs = G * (2 * kTopRows + 2 * a.tw + 2);
+    long long ublocks = (upairs + 255) / 256;
+    if (ublocks > (long long)sms * 32) ublocks = (long long)sms * 32;
+    top_union_kernel<<<(unsigned)ublocks, 256, 0, s>>>(a);
+    long long fblocks = (G * kTopSlots + 255) / 256;
+    if (fblocks > (long long)sms * 32) fblocks = (long long)sms * 32;
+    top_flatten_kernel<<<(unsigned)fblocks, 256, 0, s>>>(a);
+    top_apply_kernel<DT><<<(unsigned)cblocks, kTopThreads, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_top(const ImgDesc& d, void* scratch, unsigned long long* top_pixels, int device, cudaStream_t s,
+                       int* launches) {
+    if (d.W == 0 || d.H == 0) return cudaSuccess;
+    TopArgs a{};
+    a.d = d;
+    top_dims(d, &a.tx_n, &a.ty_n, &a.tw);
+    a.conn = d.conn;
+    const size_t G = (size_t)a.tx_n * a.ty_n, nodes = G * kTopSlots;
+    char* p = static_cast<char*>(scratch);
+    a.thr_key = reinterpret_cast<unsigned*>(p);
+    p += tal(256);
+    a.tmax = reinterpret_cast<unsigned*>(p);
+    p += tal(G * 4);
+    a.ns = reinterpret_cast<int*>(p);
+    p += tal(G * 4);
+    a.gparent = reinterpret_cast<int*>(p);
+    p += tal(nodes * 4);
+    a.gmax = reinterpret_cast<unsigned*>(p);
+    p += tal(nodes * 4);
+    a.rootidx = reinterpret_cast<unsigned short*>(p);
+    p += tal(nodes * 2);
+    a.edge = reinterpret_cast<signed char*>(p);
+    a.edge_stride = 128 + 2 * a.tw;
+    a.top_pixels = top_pixels;
+    int sms = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.thr_key, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    if (d.dtype == DT_U8)
+        e = launch_top_t<DT_U8>(a, sms, s);
+    else if (d.dtype == DT_U16)
+        e = launch_top_t<DT_U16>(a, sms, s);
+    else
+        e = launch_top_t<DT_I32>(a, sms, s);
+    if (e == cudaSuccess && launches) *launches += 5;
+    return e;
+}
+
+cudaError_t launch_seed(const ImgDesc& d, unsigned* state, unsigned* list, unsigned* nlist, cudaStream_t s,
+                        int* launches) {
+    if (d.W == 0 || d.H == 0) return cudaSuccess;
+    const long long tiles = (long long)d.tiles_x * d.tiles_y;
+    long long blocks = (tiles * 32 + 255) / 256;
+    if (blocks > 152ll * 16) blocks = 152ll * 16;
+    if (blocks < 1) blocks = 1;
+    if (d.dtype == DT_U8)
+        seed_kernel<DT_U8><<<(unsigned)blocks, 256, 0, s>>>(d, state, list, nlist);
+    else if (d.dtype == DT_U16)
+        seed_kernel<DT_U16><<<(unsigned)blocks, 256, 0, s>>>(d, state, list, nlist);
+    else
+        seed_kernel<DT_I32><<<(unsigned)blocks, 256, 0, s>>>(d, state, list, nlist);
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
+
+}  // namespace iwpp

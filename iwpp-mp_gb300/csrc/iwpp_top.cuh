@@ -1,0 +1,24 @@
+// iwpp_top.cuh -- the front stage (iwpp_top.cu): reconstruction of the
+// image's top level set by connected-component labelling, and the check that
+// seeds the tile engine after the whole-image passes.
+#pragma once
+
+#include "iwpp_device.cuh"
+
+namespace iwpp {
+
+// Device scratch the top-level stage over image d needs.
+size_t top_scratch_bytes(const ImgDesc& d);
+// Enqueues the top-level stage over image d: the pixels whose mask is at the
+// image's largest value rise to the largest marker (capped at that value) of
+// their connected set of such pixels.  *top_pixels (device) counts the
+// pixels labelled.  `launches` (nullable) counts the kernels launched.
+cudaError_t launch_top(const ImgDesc& d, void* scratch, unsigned long long* top_pixels, int device, cudaStream_t s,
+                       int* launches);
+// Marks every engine tile of image d (tile height d.tile_rows) that holds a
+// pixel a neighbour could raise DIRTY in `state` (others 0) and appends its
+// global id to `list`, counting in *nlist.
+cudaError_t launch_seed(const ImgDesc& d, unsigned* state, unsigned* list, unsigned* nlist, cudaStream_t s,
+                        int* launches);
+
+}  // namespace iwpp

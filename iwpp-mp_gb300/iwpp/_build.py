@@ -21,9 +21,9 @@ REPO_DIR = os.path.dirname(os.path.dirname(PKG_DIR))
 INCLUDE_DIR = os.path.join(REPO_DIR, "include")
 LIB_DIR = os.path.join(PKG_DIR, "lib")
 
-CUDA_SOURCES = ["iwpp_engine.cu", "iwpp_sweeps.cu", "iwpp_front.cu", "iwpp_api.cu", "iwpp_noalloc.cu",
+CUDA_SOURCES = ["iwpp_engine.cu", "iwpp_sweeps.cu", "iwpp_top.cu", "iwpp_api.cu", "iwpp_noalloc.cu",
                 "iwpp_server.cu", "iwpp_tune.cu"]
-CUDA_HEADERS = ["iwpp_device.cuh", "iwpp_engine.cuh", "iwpp_front.cuh", "iwpp_tune.h"]
+CUDA_HEADERS = ["iwpp_device.cuh", "iwpp_engine.cuh", "iwpp_top.cuh", "iwpp_tune.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
                      "-I" + INCLUDE_DIR]

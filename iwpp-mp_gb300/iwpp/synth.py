@@ -180,10 +180,11 @@ def config3_specs(n: int = 64, seed: int = 3):
     return specs
 
 
-def config4_stream(n_requests: int = 4000, pool: int = 48, seed: int = 4, rate: float = 2000.0):
+def config4_stream(n_requests: int = 4000, pool: int = 128, seed: int = 4, rate: float = 2000.0):
     """(arrival_times_s, request -> spec index, specs).  Requests draw their
-    image from a pool of `pool` distinct specs (synthesising thousands of
-    multi-megapixel images per run is out of reach on the host)."""
+    image from a pool of `pool` distinct specs, each with its own seed
+    (synthesising and checking thousands of multi-megapixel images per run
+    is out of reach on the host: 128 take about half a minute)."""
     r = random.Random(seed)
     specs = []
     for i in range(pool):

@@ -48,8 +48,9 @@ def test_front_random_shapes(dt, conn, variant):
         out, st = run(marker, mask, conn, variant)
         assert st.status == 0
         assert np.array_equal(out, ref), (h, w, int((out != ref).sum()))
-        if h * w > 1000:
-            assert st.front_sweeps >= 4
+        # the top-level stage (5 kernels), four whole-image passes, the seed
+        # check and the engine ran
+        assert st.launches >= 5 + 16 + 3
 
 
 @pytest.mark.parametrize("variant", VARIANTS)

@@ -215,6 +215,33 @@ def test_whole_image_sweeps_match_restatement(dt, conn):
 
 
 @pytest.mark.parametrize("dt", [0, 1, 2])
+@pytest.mark.parametrize("width", [333, 1000, 4099])
+def test_horizontal_sweeps_of_16_byte_rows(dt, width):
+    # rows starting on 16-byte boundaries take the 16-byte-lane horizontal
+    # sweep; the row's last lane is partial.  The padding after each row holds
+    # the type's largest value in both planes: a read past the row's end
+    # would raise pixels the oracle leaves.
+    torch = _torch()
+    h = 37
+    mask = synth.noise_mask(width, h, dt, 23, 3.0, 5)
+    marker = synth.sparse_marker(mask, 7, 0.002)
+    pw = (width + 15) // 16 * 16 + 16
+    top = np.iinfo(NP[dt]).max
+    for d in (0, 2):
+        for conn in (4, 8):
+            bm = np.full((h, pw), top, NP[dt])
+            bk = np.full((h, pw), top, NP[dt])
+            bm[:, :width] = marker
+            bk[:, :width] = mask
+            tm, tk = to_dev(bm), to_dev(bk)
+            iwpp.sweep(tm[:, :width], tk[:, :width], d, conn)
+            torch.cuda.synchronize()
+            out = from_dev(tm, NP[dt])
+            assert np.array_equal(out[:, :width], oracle.sweep(marker, mask, d, conn)), (d, conn)
+            assert (out[:, width:] == top).all()
+
+
+@pytest.mark.parametrize("dt", [0, 1, 2])
 @pytest.mark.parametrize("shape", [(2500, 131), (4500, 64)])
 def test_vertical_sweeps_of_tall_images(dt, shape):
     # more than two segments of rows: the segmented vertical sweep
