@@ -844,13 +844,33 @@ def main():
                     help="distinct generated image pairs the served requests draw from")
     ap.add_argument("--lanes", type=int, default=3)
     ap.add_argument("--spiral-reps", type=int, default=3)
+    ap.add_argument("--config1-only", action="store_true",
+                    help="only the six 4096^2 configuration-1 reconstructions with --variant (one JSON line)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     import __graft_entry__ as ge
 
     ge.build()
+    if args.config1_only:
+        return run_config1_only(args)
     return run_ours(args)
+
+
+def run_config1_only(args):
+    """The configuration-1 sub-result alone, for one queue variant (the form
+    the per-variant profiles are captured with)."""
+    import torch
+
+    import iwpp
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    handle = iwpp.Handle(0)
+    res = bench_config1(args, dev, args.variant, handle)
+    handle.close()
+    print(json.dumps({"config1": res}), flush=True)
+    return 0
 
 
 if __name__ == "__main__":

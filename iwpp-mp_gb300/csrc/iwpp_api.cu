@@ -656,7 +656,7 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
                 static const int order[4] = {0, 1, 2, 3};
                 ImgDesc dv = d;
                 dv.conn = 4;
-                e = launch_sweep(dv, order[dir], s, base + l.off_sweep, &nl);
+                e = launch_sweep(dv, order[dir], s, base + l.off_sweep, &nl, &a.ctrl->error);
                 if (e != cudaSuccess) return cuda_status(e);
             }
     if (front) {

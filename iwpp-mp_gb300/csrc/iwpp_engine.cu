@@ -54,14 +54,6 @@ struct WarpCounters {
 };
 
 // ---------------------------------------------------------------- mutex
-__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 
 // The global mutex (IWPP MP/src/globalQueue.cu:35, :114, a CAS spin without
 // a bound) as a ticket lock: one atomic per acquisition instead of a CAS

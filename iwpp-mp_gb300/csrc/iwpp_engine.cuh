@@ -111,11 +111,11 @@ cudaError_t launch_fixed_point_check(const ImgDesc& d, unsigned long long* count
 // out[1] ids with a wrong count, out[2] the smallest such id.
 cudaError_t queue_selftest(const EngineArgs& a, int variant, int copies, unsigned* hist, unsigned long long* out,
                            int device, cudaStream_t s);
-// Whole-image sweep; 4-connected vertical sweeps of tall uint8 / uint16
-// images use `scratch` (sweep_scratch_bytes(d) bytes, nullable) to split the
-// columns into segments.
+// Whole-image sweep; 4-connected vertical sweeps use `scratch`
+// (sweep_scratch_bytes(d) bytes, nullable) for the single-pass form, whose
+// bounded waits set *err (nullable) to 3 when they run out.
 // `launches` (nullable) is incremented by the number of kernels launched.
 cudaError_t launch_sweep(const ImgDesc& d, int direction, cudaStream_t s, void* scratch = nullptr,
-                         int* launches = nullptr);
+                         int* launches = nullptr, unsigned* err = nullptr);
 size_t sweep_scratch_bytes(const ImgDesc& d);
 }  // namespace iwpp

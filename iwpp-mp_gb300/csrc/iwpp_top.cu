@@ -30,9 +30,12 @@
 //      global union-find (link the larger root under the smaller).
 //   4. top_flatten_kernel: every node to its root; each root's gmax the
 //      largest of its component.
-//   5. top_apply_kernel: the local labelling again (the roots are the least
-//      pixel indices, so it is the same), each top-level pixel raised to its
-//      component's value.
+//   5. top_apply_list_kernel (a warp per tile): each top-level pixel of a
+//      tile with at most kTopListCap of them raised to its component's
+//      value, from the (pixel, slot) list the local kernel saved;
+//      top_apply_label_kernel (a CTA per tile with more): the local
+//      labelling again (the roots are the least pixel indices, so it is the
+//      same), then the same raise.
 #include "iwpp_engine.cuh"
 #include "iwpp_top.cuh"
 
@@ -41,6 +44,7 @@ namespace iwpp {
 constexpr int kTopRows = 64;    // rows of a tile (tiles are 128 bytes wide)
 constexpr int kTopSlots = 64;   // component nodes one tile can export
 constexpr int kTopThreads = 256;
+constexpr int kTopListCap = 256;  // (pixel, slot) entries a tile saves for the apply step
 
 // Order-preserving unsigned key of a pixel value (int32 with its sign bit
 // flipped), and back.
@@ -59,6 +63,9 @@ struct TopArgs {
     unsigned short* rootidx; // per node: the component's least pixel index in its tile
     signed char* edge;       // per tile: left (64), right (64), top (tw), bottom (tw) slot or -1
     int edge_stride;         // 128 + 2 * tw
+    int* tn;                 // per tile: its top-level pixels
+    unsigned* tlist;         // per tile: kTopListCap entries, pixel | slot << 16 (slot 0xff: none)
+    int aligned16;           // mask rows start on 16-byte boundaries
     unsigned long long* top_pixels;  // the job's count of pixels labelled
 };
 
@@ -114,6 +121,31 @@ __device__ __forceinline__ void s_union(int* parent, int a, int b) {
 }
 
 // ------------------------------------------------------------ 1. maxima
+// Largest key of a word's pixels (pixels past the row end hold the type's
+// least value, key 0).
+template <int DT>
+__device__ __forceinline__ uint32_t word_max_key(uint32_t w) {
+    if (DT == DT_U8) {
+        const uint32_t h = __vmaxu4(w, w >> 16);
+        return max(h & 0xffu, (h >> 8) & 0xffu);
+    } else if (DT == DT_U16) {
+        return max(w & 0xffffu, w >> 16);
+    } else {
+        return w ^ 0x80000000u;
+    }
+}
+
+// Per-lane running maximum of a word into `acc` (byte / half-word lanes
+// for uint8 / uint16, signed for int32).
+template <int DT>
+__device__ __forceinline__ uint32_t word_max(uint32_t acc, uint32_t w) {
+    if (DT == DT_U8) return __vmaxu4(acc, w);
+    if (DT == DT_U16) return __vmaxu2(acc, w);
+    return (uint32_t)max((int)acc, (int)w);
+}
+
+// One warp per tile; with 16-byte rows each lane reads 16 bytes of a row
+// (8 lanes a row, 4 rows per step), else one word of each row.
 template <int DT>
 __global__ void top_max_kernel(TopArgs a) {
     using P = Px<DT>;
@@ -126,19 +158,38 @@ __global__ void top_max_kernel(TopArgs a) {
     for (long long t = wg; t < G; t += nw) {
         const int ty = (int)(t / a.tx_n), tx = (int)(t - (long long)ty * a.tx_n);
         const int y0 = ty * kTopRows, rows = min(kTopRows, d.H - y0);
-        const long long byte0 = (long long)tx * 128 + lane * 4;
-        const int npx = byte0 < row_bytes ? (int)min((long long)P::PPW, (row_bytes - byte0) / P::BPP) : 0;
-        uint32_t best = 0u;  // keys: 0 is at or below every pixel
-        if (npx > 0)
-            for (int r = 0; r < rows; ++r) {
-                const uint32_t kw = load_word_plain<DT>(d.mask + (size_t)(y0 + r) * d.pitch_k + byte0, npx, false);
-                uint32_t k[P::PPW];
-                P::unpack(kw, k);
+        uint32_t acc = P::MINW;
+        if (a.aligned16) {
+            const long long byte0 = (long long)tx * 128 + (lane & 7) * 16;
+            if (byte0 < row_bytes) {
+                const bool full = byte0 + 16 <= row_bytes;
+#pragma unroll 4
+                for (int r = lane >> 3; r < rows; r += 4) {
+                    const unsigned char* src = d.mask + (size_t)(y0 + r) * d.pitch_k + byte0;
+                    if (full) {
+                        const uint4 v = __ldg(reinterpret_cast<const uint4*>(src));
+                        acc = word_max<DT>(word_max<DT>(acc, v.x), word_max<DT>(word_max<DT>(v.y, v.z), v.w));
+                    } else {
 #pragma unroll
-                for (int j = 0; j < P::PPW; ++j)
-                    if (j < npx) best = max(best, top_key<DT>(k[j]));
+                        for (int w = 0; w < 4; ++w) {
+                            const long long b = byte0 + w * 4;
+                            if (b < row_bytes)
+                                acc = word_max<DT>(acc, load_word_plain<DT>(src + w * 4,
+                                                                            (int)((row_bytes - b) / P::BPP), false));
+                        }
+                    }
+                }
             }
-        best = __reduce_max_sync(FULL, best);
+        } else {
+            const long long byte0 = (long long)tx * 128 + lane * 4;
+            if (byte0 < row_bytes) {
+                const int npx = (int)min((long long)P::PPW, (row_bytes - byte0) / P::BPP);
+                for (int r = 0; r < rows; ++r)
+                    acc = word_max<DT>(acc, load_word_plain<DT>(d.mask + (size_t)(y0 + r) * d.pitch_k + byte0, npx,
+                                                                false));
+            }
+        }
+        const uint32_t best = __reduce_max_sync(FULL, word_max_key<DT>(acc));
         if (lane == 0) {
             a.tmax[t] = best;
             atomicMax(a.thr_key, best);
@@ -337,11 +388,18 @@ __global__ void __launch_bounds__(kTopThreads) top_local_kernel(TopArgs a) {
             const int root = sm.parent[p];
             e[i] = root < 0 ? (signed char)-1 : sm.slot[root];
         }
+        // the (pixel, slot) list for the apply step, when it fits
+        if (n <= kTopListCap)
+            for (int q = threadIdx.x; q < n; q += blockDim.x) {
+                const int p = sm.list[q];
+                a.tlist[t * kTopListCap + q] = (unsigned)p | ((unsigned)(unsigned char)sm.slot[sm.parent[p]] << 16);
+            }
         __syncthreads();
         const int ns = min(sm.nslots, kTopSlots);
         for (int q = threadIdx.x; q < ns; q += blockDim.x) a.gmax[t * kTopSlots + q] = sm.sval[q];
         if (threadIdx.x == 0) {
             a.ns[t] = ns;
+            a.tn[t] = n;
             atomicAdd(a.top_pixels, (unsigned long long)n);
         }
         __syncthreads();
@@ -434,8 +492,39 @@ __global__ void top_flatten_kernel(TopArgs a) {
 }
 
 // ------------------------------------------------------------ 5. apply
+// Tiles whose list was saved: a warp per tile, a lane per entry; the nodes
+// point at their roots after the flatten step.
 template <int DT>
-__global__ void __launch_bounds__(kTopThreads) top_apply_kernel(TopArgs a) {
+__global__ void top_apply_list_kernel(TopArgs a) {
+    using P = Px<DT>;
+    constexpr int TW = 32 * P::PPW;
+    const int lane = threadIdx.x & 31;
+    const ImgDesc& d = a.d;
+    const unsigned tkey = *(const volatile unsigned*)a.thr_key;
+    const long long G = (long long)a.tx_n * a.ty_n;
+    const long long wg = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long t = wg; t < G; t += nw) {
+        if (a.tmax[t] < tkey) continue;
+        const int n = a.tn[t];
+        if (n > kTopListCap) continue;
+        const int ty = (int)(t / a.tx_n), tx = (int)(t - (long long)ty * a.tx_n);
+        for (int e = lane; e < n; e += 32) {
+            const unsigned u = a.tlist[t * kTopListCap + e];
+            const unsigned s = u >> 16;
+            if (s >= (unsigned)kTopSlots) continue;
+            const int p = (int)(u & 0xffffu), r = p / TW, c = p - r * TW;
+            const uint32_t v = top_key<DT>(__ldcg(&a.gmax[__ldcg(&a.gparent[t * kTopSlots + s])]));
+            unsigned char* px = d.marker + (size_t)(ty * kTopRows + r) * d.pitch_m + (size_t)(tx * TW + c) * P::BPP;
+            if (P::gt(v, P::ld_px(px))) P::st_px(px, v);
+        }
+    }
+}
+
+// Tiles with more top-level pixels than the list holds: a CTA per tile
+// labels the tile again.
+template <int DT>
+__global__ void __launch_bounds__(kTopThreads) top_apply_label_kernel(TopArgs a) {
     using P = Px<DT>;
     constexpr int TW = 32 * P::PPW;
     extern __shared__ __align__(16) unsigned char top_smem[];
@@ -444,7 +533,7 @@ __global__ void __launch_bounds__(kTopThreads) top_apply_kernel(TopArgs a) {
     const unsigned tkey = *(const volatile unsigned*)a.thr_key;
     const long long G = (long long)a.tx_n * a.ty_n;
     for (long long t = blockIdx.x; t < G; t += gridDim.x) {
-        if (a.tmax[t] < tkey) continue;
+        if (a.tmax[t] < tkey || a.tn[t] <= kTopListCap) continue;
         const int ty = (int)(t / a.tx_n), tx = (int)(t - (long long)ty * a.tx_n);
         const unsigned bits = label_tile<DT>(a, tx, ty, tkey, sm);
         const int n = sm.nlist;
@@ -613,7 +702,7 @@ size_t top_scratch_bytes(const ImgDesc& d) {
     top_dims(d, &tx_n, &ty_n, &tw);
     const size_t G = (size_t)tx_n * ty_n, nodes = G * kTopSlots;
     return tal(256) + tal(G * 4) + tal(G * 4) + tal(nodes * 4) + tal(nodes * 4) + tal(nodes * 2) +
-           tal(G * (128 + 2 * (size_t)tw));
+           tal(G * (128 + 2 * (size_t)tw)) + tal(G * 4) + tal(G * kTopListCap * 4);
 }
 
 template <int DT>
@@ -621,7 +710,7 @@ static cudaError_t launch_top_t(const TopArgs& a, int sms, cudaStream_t s) {
     const size_t smem = sizeof(TopSmem<DT>);
     cudaError_t e = cudaFuncSetAttribute(top_local_kernel<DT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(top_apply_kernel<DT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(top_apply_label_kernel<DT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const long long G = (long long)a.tx_n * a.ty_n;
     long long wblocks = (G * 32 + 255) / 256;
@@ -636,7 +725,8 @@ static cudaError_t launch_top_t(const TopArgs& a, int sms, cudaStream_t s) {
     long long fblocks = (G * kTopSlots + 255) / 256;
     if (fblocks > (long long)sms * 32) fblocks = (long long)sms * 32;
     top_flatten_kernel<<<(unsigned)fblocks, 256, 0, s>>>(a);
-    top_apply_kernel<DT><<<(unsigned)cblocks, kTopThreads, smem, s>>>(a);
+    top_apply_list_kernel<DT><<<(unsigned)wblocks, 256, 0, s>>>(a);
+    top_apply_label_kernel<DT><<<(unsigned)cblocks, kTopThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -663,6 +753,11 @@ cudaError_t launch_top(const ImgDesc& d, void* scratch, unsigned long long* top_
     p += tal(nodes * 2);
     a.edge = reinterpret_cast<signed char*>(p);
     a.edge_stride = 128 + 2 * a.tw;
+    p += tal(G * (size_t)a.edge_stride);
+    a.tn = reinterpret_cast<int*>(p);
+    p += tal(G * 4);
+    a.tlist = reinterpret_cast<unsigned*>(p);
+    a.aligned16 = (reinterpret_cast<uintptr_t>(d.mask) & 15u) == 0u && (d.pitch_k & 15) == 0;
     a.top_pixels = top_pixels;
     int sms = 0;
     cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -674,7 +769,7 @@ cudaError_t launch_top(const ImgDesc& d, void* scratch, unsigned long long* top_
         e = launch_top_t<DT_U16>(a, sms, s);
     else
         e = launch_top_t<DT_I32>(a, sms, s);
-    if (e == cudaSuccess && launches) *launches += 5;
+    if (e == cudaSuccess && launches) *launches += 6;
     return e;
 }
 

@@ -1,6 +1,7 @@
-"""GPU parity of the front passes (iwpp_config.front_passes = 1): whole-image
-directional sweeps restricted to the tiles that changed, then the seed check
-and the tile engine from the tiles still violating a constraint.  Every
+"""GPU parity of the front stage (iwpp_config.front_passes = 1): the pixels at
+the mask's largest value raised by connected-component labelling, four
+whole-image passes, then the seed check and the tile engine from the tiles
+still violating a constraint.  Every
 result must equal the CPU oracle bit for bit, for every pixel type,
 connectivity and queue variant, on ragged and degenerate shapes, unclipped
 markers, padded pitches, batches and graph plans."""
@@ -48,9 +49,9 @@ def test_front_random_shapes(dt, conn, variant):
         out, st = run(marker, mask, conn, variant)
         assert st.status == 0
         assert np.array_equal(out, ref), (h, w, int((out != ref).sum()))
-        # the top-level stage (5 kernels), four whole-image passes, the seed
+        # the top-level stage (6 kernels), four whole-image passes, the seed
         # check and the engine ran
-        assert st.launches >= 5 + 16 + 3
+        assert st.launches >= 6 + 16 + 3
 
 
 @pytest.mark.parametrize("variant", VARIANTS)
@@ -66,6 +67,41 @@ def test_front_spirals_and_config0(variant):
     ref = oracle.reconstruct(marker, mask, 8)
     out, _ = run(marker, mask, 8, variant)
     assert np.array_equal(out, ref)
+
+
+@pytest.mark.parametrize("dt", [0, 1, 2])
+@pytest.mark.parametrize("conn", [4, 8])
+def test_front_top_level_plateaus_and_corridors(dt, conn):
+    # the top level as a dense plateau (labelling tiles with more top pixels
+    # than their saved list holds are labelled again), as one-pixel
+    # corridors crossing many tiles (tiles whose list is saved), and as
+    # isolated pixels; a labelling tile with more components than node slots
+    # (a checkerboard of single pixels) keeps the extra ones for the passes
+    rng = np.random.default_rng(40 + dt * 2 + conn)
+    info = np.iinfo(NP[dt])
+    h, w = 700, 1500
+    top = info.max
+    mask = rng.integers(info.min // 2 if dt == 2 else 0, top // 2, (h, w), dtype=np.int64).astype(NP[dt])
+    mask[100:260, 200:560] = top                                 # plateau
+    mask[400, 10:1490] = top                                     # horizontal corridor
+    mask[300:690, 1200] = top                                    # vertical corridor
+    mask[400:690, 700] = top                                     # corridor meeting the first
+    yy, xx = np.mgrid[0:64, 0:128]
+    mask[512:576, 896:1024][((yy + xx) % 2 == 0)[:, :128]] = top  # checkerboard: > 64 components
+    mask[5, 5] = top                                             # isolated
+    marker = np.full((h, w), info.min if dt == 2 else 0, NP[dt])
+    marker[150, 300] = top - 7
+    marker[400, 1480] = top - 3
+    marker[689, 700] = top - 1
+    marker[520, 900] = top - 5
+    marker[rng.integers(0, h, 50), rng.integers(0, w, 50)] = top // 3
+    marker = np.minimum(marker, mask)
+    ref = oracle.reconstruct(marker, mask, conn)
+    for variant in ("unique", "async"):
+        out, st = run(marker, mask, conn, variant)
+        assert st.status == 0
+        assert np.array_equal(out, ref), (variant, int((out != ref).sum()))
+        assert st.top_pixels == int((mask == top).sum())
 
 
 @pytest.mark.parametrize("tile_rows", [32, 64])
