@@ -76,8 +76,14 @@ typedef struct iwpp_config {
                                   raised by connected-component labelling, init_passes
                                   whole-image passes (default 4), and the tile engine started
                                   from the tiles still holding a pixel a neighbour can raise:
-                                  0 = default (the tuning table's choice, else the tile engine
-                                  alone), 1 = always, 2 = never */
+                                  0 = default (the tuning table's choice, else 3 when the job's
+                                  largest image has 2^26 pixels or more and 2 below that),
+                                  1 = always, 2 = never, 3 = decided on the device per job: a
+                                  seed check over the untouched images measures the initial
+                                  front, and fewer than one tile in 64 with a pixel a neighbour
+                                  can raise (a few sparse seeds: long propagation paths) takes
+                                  the stage, more leaves the job to the engine (seeded from that
+                                  check) */
     int phantom_work;          /* fault-injection hook for tests, 0 normally.  1: the job counts
                                   one unit of work that never arrives (a queue entry nobody
                                   inserts; for the round-based queues a CTA that never reaches
@@ -105,6 +111,7 @@ typedef struct iwpp_stats {
     long long phase_cycles[5];
     long long launches;    /* kernels this library launched for the job */
     long long top_pixels;   /* pixels the top-level stage labelled (0 without it) */
+    long long front_stage;  /* 1: the job ran the front stage, 0: the tile engine alone */
 } iwpp_stats;
 
 /* One image of a batch. */
@@ -197,7 +204,8 @@ IWPP_API int iwpp_queue_selftest(int device, int variant, int grid_side, int cop
 typedef struct iwpp_tune_result {
     iwpp_config best;  /* fastest configuration */
     double best_ms;    /* its median device time */
-    double default_ms; /* median device time of the untuned default (64 rows, automatic solver) */
+    double default_ms; /* median device time of the untuned default (default tile height, automatic
+                          solver; front_passes 3 with 4 passes for images of 2^26 pixels or more) */
     int candidates;    /* configurations timed */
     int reserved;
 } iwpp_tune_result;

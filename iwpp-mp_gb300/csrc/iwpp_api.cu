@@ -75,7 +75,7 @@ Config resolve_config(const iwpp_config* c) {
     r.clip_marker = c ? c->clip_marker : 0;
     r.plain_loads = c ? c->plain_loads : 0;
     r.solver = c && c->solver >= 0 && c->solver <= 2 ? c->solver : 0;
-    r.front_passes = c && c->front_passes >= 0 && c->front_passes <= 2 ? c->front_passes : 0;
+    r.front_passes = c && c->front_passes >= 0 && c->front_passes <= 3 ? c->front_passes : 0;
     r.phantom_work = c && c->phantom_work == 1 ? 1 : 0;
     r.dflt_tile = r.tile_rows == 0;
     r.dflt_queue = r.queue_capacity == 0;
@@ -223,14 +223,28 @@ Layout layout_for(long long n_imgs, long long G, long long cap, bool two_queues,
     return l;
 }
 
-// Whole-image passes after the front passes when the caller leaves
+// Whole-image passes after the top-level stage when the caller leaves
 // init_passes at its default: measured on the 16384^2 spiral, four leave
-// about a tenth of the tiles to the engine.
+// about a fifth of the tiles to the engine and two or eight cost more.
 constexpr int kFrontFullPasses = 4;
+// Untuned jobs whose largest image has at least this many pixels decide on
+// the device whether to take the front stage (front_passes 3): the seed
+// check over the untouched images measures the initial front, and a small
+// one (a few sparse seeds) means long propagation paths, which the tile
+// engine alone walks one dependent tile visit at a time (the 16384^2
+// spiral: 235 ms alone, 4 ms with the stage) while a large one is
+// short-range work the engine does faster alone (16384^2 h-dome: 3.4 ms
+// alone, 6.5 ms with the stage).  The check and the skipped launches cost
+// about 0.1 ms, too much below this size (six 4096^2 h-dome images take
+// 0.24-0.73 ms each).
+constexpr long long kFrontDefaultPixels = 1ll << 26;
+
+// The job runs the front stage always (1) or as the device decides (3).
+bool job_front(const Config& c) { return c.front_passes == 1 || c.front_passes == 3; }
 
 // Whole-image raster / anti-raster passes a job runs before the engine.
 int job_full_passes(const Config& c) {
-    if (c.front_passes == 1 && c.dflt_init) return kFrontFullPasses;
+    if (job_front(c) && c.dflt_init) return kFrontFullPasses;
     return c.init_passes;
 }
 
@@ -283,7 +297,7 @@ long long job_queue_capacity(const Job& job) {
 // The workspace layout of a job (the same for direct calls and plans).
 Layout job_layout(const Job& job) {
     const bool two = job.variant == IWPP_QUEUE_DOUBLE || job.variant == IWPP_QUEUE_UNIQUE;
-    const bool front = job.cfg.front_passes == 1;
+    const bool front = job_front(job.cfg);
     size_t sweep = 0;
     for (const auto& d : job.descs) {
         if (job_full_passes(job.cfg) > 0) {
@@ -328,8 +342,15 @@ int build_job(Job& job, const iwpp_image* imgs, int n, int variant, const iwpp_c
                 job.cfg.dflt_init = false;  // the table's count stands, also with front passes
             }
             if (job.cfg.dflt_queue && e.queue_mult > 0) job.cfg.queue_capacity = -(long long)e.queue_mult;
-            if (job.cfg.dflt_front) job.cfg.front_passes = e.front_passes ? 1 : 2;
+            if (job.cfg.dflt_front) job.cfg.front_passes = tune_front_code(e.front_passes);
         }
+    }
+    if (job.cfg.front_passes == 0) {
+        long long largest = 0;
+        for (int i = 0; i < n; ++i)
+            if (imgs[i].width > 0 && imgs[i].height > 0)
+                largest = std::max(largest, (long long)imgs[i].width * imgs[i].height);
+        job.cfg.front_passes = largest >= kFrontDefaultPixels ? 3 : 2;
     }
     int th = job.cfg.tile_rows;
     if (th == 0) th = n > 0 ? default_tile_rows(job.variant, job_tiles64(imgs, n)) : 64;
@@ -596,11 +617,13 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
     a.max_restarts = job.cfg.max_restarts;
     a.solver = job.cfg.solver;
     a.phantom = job.cfg.phantom_work;
-    const bool front = job.cfg.front_passes == 1 && job.G > 0;
+    const bool front = job_front(job.cfg) && job.G > 0;
+    const bool gated = front && job.cfg.front_passes == 3;
     unsigned* seed_list = reinterpret_cast<unsigned*>(base + l.off_list);
     unsigned* seed_count = seed_list + job.G;
     if (front) {
         a.front = 1;
+        a.front_gated = gated ? 1 : 0;
         a.init_list = seed_list;
         a.init_count = seed_count;
     }
@@ -633,21 +656,33 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
             if (e != cudaSuccess) return cuda_status(e);
             ++nl;
         }
+    // the front stage's view of the images: gated by the device's decision
+    std::vector<ImgDesc> fdescs = job.descs;
+    if (gated)
+        for (auto& d : fdescs) d.gate = &a.ctrl->front_gate;
     if (front) {
         // The top level of each image first (its connected sets of pixels at
         // the mask's largest value, however long); the whole-image passes and
         // the seed check follow.  The job's error word and top-pixel count
-        // are zeroed here: the engine's initialisation keeps them.
+        // are zeroed here: the engine's initialisation keeps them.  A gated
+        // job first measures its initial front (a seed check over the
+        // untouched images) and decides.
         Ctrl* c = a.ctrl;
         e = cudaMemsetAsync(&c->error, 0, sizeof(c->error), s);
         if (e == cudaSuccess) e = cudaMemsetAsync(&c->top_pixels, 0, sizeof(c->top_pixels), s);
-        for (size_t i = 0; i < job.descs.size() && e == cudaSuccess; ++i)
-            e = launch_top(job.descs[i], base + l.off_sweep, &c->top_pixels, device, s, &nl);
+        if (gated) {
+            if (e == cudaSuccess) e = cudaMemsetAsync(seed_count, 0, sizeof(unsigned), s);
+            for (size_t i = 0; i < job.descs.size() && e == cudaSuccess; ++i)
+                e = launch_seed(job.descs[i], a.state, seed_list, seed_count, s, &nl);
+            if (e == cudaSuccess) e = launch_front_decide(&c->front_gate, seed_count, (unsigned)job.G, s, &nl);
+        }
+        for (size_t i = 0; i < fdescs.size() && e == cudaSuccess; ++i)
+            e = launch_top(fdescs[i], base + l.off_sweep, &c->top_pixels, device, s, &nl);
         if (e != cudaSuccess) return cuda_status(e);
     }
     const int full_passes = job_full_passes(job.cfg);
     for (int p = 0; p < full_passes; ++p)
-        for (const auto& d : job.descs)
+        for (const auto& d : fdescs)
             for (int dir = 0; dir < 4; ++dir) {
                 // raster (+X, +Y) then anti-raster (-X, -Y).  The vertical
                 // sweeps take the pixel above / below only: a valid update
@@ -656,15 +691,16 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
                 static const int order[4] = {0, 1, 2, 3};
                 ImgDesc dv = d;
                 dv.conn = 4;
-                e = launch_sweep(dv, order[dir], s, base + l.off_sweep, &nl, &a.ctrl->error);
+                e = launch_sweep(dv, order[dir], s, base + l.off_sweep, &nl);
                 if (e != cudaSuccess) return cuda_status(e);
             }
     if (front) {
         // the tile engine starts from the tiles still holding a pixel that a
-        // neighbour can raise
-        e = cudaMemsetAsync(seed_count, 0, sizeof(unsigned), s);
-        for (size_t i = 0; i < job.descs.size() && e == cudaSuccess; ++i)
-            e = launch_seed(job.descs[i], a.state, seed_list, seed_count, s, &nl);
+        // neighbour can raise (a gated job that left the stage out keeps the
+        // list of its first check: the decision emptied it otherwise)
+        if (!gated) e = cudaMemsetAsync(seed_count, 0, sizeof(unsigned), s);
+        for (size_t i = 0; i < fdescs.size() && e == cudaSuccess; ++i)
+            e = launch_seed(fdescs[i], a.state, seed_list, seed_count, s, &nl);
         if (e != cudaSuccess) return cuda_status(e);
     }
     e = engine_launch_init(a, job.variant, s);
@@ -709,6 +745,7 @@ int read_stats(Ctrl* host_ctrl, const Workspace& ws, cudaStream_t s, long long t
         for (int i = 0; i < 5; ++i) out->phase_cycles[i] = (long long)host_ctrl->phase[i];
         out->launches = launches;
         out->top_pixels = (long long)host_ctrl->top_pixels;
+        out->front_stage = host_ctrl->front_gate != 0u ? 1 : 0;
     }
     return st;
 }
@@ -951,6 +988,7 @@ int iwpp_handle_sync(iwpp_handle h, iwpp_stats* stats) {
         for (int i = 0; i < 5; ++i) stats->phase_cycles[i] = (long long)c.phase[i];
         stats->launches = h->last_launches;
         stats->top_pixels = (long long)c.top_pixels;
+        stats->front_stage = c.front_gate != 0u ? 1 : 0;
     }
     return set_last(st);
 }
@@ -1069,6 +1107,7 @@ int iwpp_plan_sync(iwpp_plan p, iwpp_stats* stats) {
         for (int i = 0; i < 5; ++i) stats->phase_cycles[i] = (long long)c.phase[i];
         stats->launches = p->launches;
         stats->top_pixels = (long long)c.top_pixels;
+        stats->front_stage = c.front_gate != 0u ? 1 : 0;
     }
     return set_last(st);
 }
@@ -1224,19 +1263,34 @@ int iwpp_autotune(iwpp_handle h, const iwpp_image* images, int n, int variant, i
         }
     };
     if (rc == IWPP_OK) {
-        // stage 1: tile height x in-tile solver, no initial passes
+        // the untuned default first when it is the front stage (large
+        // images), then stage 1: tile height x in-tile solver, no passes
         const int dflt_th = default_tile_rows(v, job_tiles64(images, n));
+        long long largest = 0;
+        for (int i = 0; i < n; ++i)
+            if (images[i].width > 0 && images[i].height > 0)
+                largest = std::max(largest, (long long)images[i].width * images[i].height);
+        const bool front_default = largest >= kFrontDefaultPixels;
+        if (front_default) {
+            // (the front stage as the device decides, with its default passes)
+            iwpp_config c{};
+            c.tile_rows = dflt_th;
+            c.init_passes = kFrontFullPasses;
+            c.front_passes = 3;
+            consider(c, true);
+        }
         for (int th : {64, 32})
             for (int solver : {0, 1, 2}) {
                 iwpp_config c{};
                 c.tile_rows = th;
                 c.solver = solver;
                 c.init_passes = 0;
-                consider(c, th == dflt_th && solver == 0);
+                c.front_passes = 2;
+                consider(c, !front_default && th == dflt_th && solver == 0);
             }
-        // stage 2: front passes (directional sweeps restricted to the tiles
-        // that changed, until nothing changes) before the tile engine, with
-        // the best tile height and solver; long propagation paths want them
+        // stage 2: the front stage (top-level labelling, then 2 / 4 / 8
+        // whole-image passes, then the engine from the seed check) with the
+        // best tile height and solver; long propagation paths want it
         if (best_ms >= 0.0) {
             const iwpp_config base = best;
             for (int ip : {2, 4, 8}) {
@@ -1250,7 +1304,7 @@ int iwpp_autotune(iwpp_handle h, const iwpp_image* images, int n, int variant, i
         // anti-raster passes, doubling while they pay (long corridors want
         // one pass per turn of the front), stopping at the first count that
         // does not beat the best
-        if (best_ms >= 0.0 && best.front_passes != 1) {
+        if (best_ms >= 0.0 && best.front_passes != 1 && best.front_passes != 3) {
             const iwpp_config base = best;
             for (int ip = 1; ip <= 64; ip *= 2) {
                 iwpp_config c = base;
@@ -1283,7 +1337,7 @@ int iwpp_autotune(iwpp_handle h, const iwpp_image* images, int n, int variant, i
         }
         if (!dts.empty()) {
             TuneEntry e{best.tile_rows, best.solver, best.init_passes,
-                        best.queue_capacity < 0 ? (int)-best.queue_capacity : 0, best.front_passes == 1 ? 1 : 0};
+                        best.queue_capacity < 0 ? (int)-best.queue_capacity : 0, tune_front_store(best.front_passes)};
             tune_store(tune_key(v, dts.data(), cns.data(), pxs.data(), (int)dts.size()), e);
         }
         // leave the images reconstructed (with the winner)

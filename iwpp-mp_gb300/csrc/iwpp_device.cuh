@@ -125,7 +125,15 @@ struct ImgDesc {
     int tiles_x, tiles_y;
     int tile_base;  // first global tile index of this image
     int tile_rows;  // TH used for this image
+    // Nullable.  The front-stage kernels (top-level labelling, whole-image
+    // passes, seed check) over this image return at once while *gate is 0:
+    // the job decided on the device to leave the image to the tile engine.
+    const unsigned* gate;
 };
+
+__device__ __forceinline__ bool gated_off(const ImgDesc& d) {
+    return d.gate != nullptr && *(const volatile unsigned*)d.gate == 0u;
+}
 
 // neighbour direction bits returned by a tile visit
 enum : unsigned {
@@ -203,6 +211,29 @@ __device__ __forceinline__ long long globaltimer_ns() {
     long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
+}
+
+// ------------------------------------------------ packed-word min / max
+// Per-pixel max / min of two packed words (uint8: four bytes, uint16: two
+// halves, int32: one signed value), and whether some pixel of a is above
+// the same pixel of b.
+template <int DT>
+__device__ __forceinline__ uint32_t word_max(uint32_t a, uint32_t b) {
+    if (DT == DT_U8) return __vmaxu4(a, b);
+    if (DT == DT_U16) return __vmaxu2(a, b);
+    return (uint32_t)max((int)a, (int)b);
+}
+template <int DT>
+__device__ __forceinline__ uint32_t word_min(uint32_t a, uint32_t b) {
+    if (DT == DT_U8) return __vminu4(a, b);
+    if (DT == DT_U16) return __vminu2(a, b);
+    return (uint32_t)min((int)a, (int)b);
+}
+template <int DT>
+__device__ __forceinline__ bool word_any_gt(uint32_t a, uint32_t b) {
+    if (DT == DT_U8) return __vcmpgtu4(a, b) != 0u;
+    if (DT == DT_U16) return __vcmpgtu2(a, b) != 0u;
+    return (int)a > (int)b;
 }
 
 // ------------------------------------------------ clamp-map scan steps
@@ -393,12 +424,30 @@ __device__ __forceinline__ unsigned long long vpass(WarpSmem<TH>& sm, int lane, 
     using P = Px<DT>;
     constexpr int N = P::PPW;
     const int first = DOWN ? __ffsll((long long)dirty) : 64 - __clzll((long long)dirty);
-    uint32_t prev[N];
-    P::unpack(sm.tm[(DOWN ? first - 1 : first + 1) * 32 + lane], prev);
     const int count = DOWN ? TH - first + 1 : first;
     steps += (unsigned)count;
     unsigned long long chg = 0ull;
     uint32_t diff = 0u;
+    if (CONN == 4) {
+        // columns are independent: one packed min / max per word and row
+        uint32_t prevw = sm.tm[(DOWN ? first - 1 : first + 1) * 32 + lane];
+#pragma unroll 4
+        for (int i = 0; i < count; ++i) {
+            const int r = DOWN ? first + i : first - i;
+            const uint32_t old = sm.tm[r * 32 + lane];
+            const uint32_t nw = word_max<DT>(old, word_min<DT>(prevw, sm.tk[r * 32 + lane]));
+            sm.tm[r * 32 + lane] = nw;
+            const uint32_t x = nw ^ old;
+            diff |= x;
+            if (x != 0u) chg |= 1ull << (r - 1);
+            prevw = nw;
+        }
+        col_now |= (diff & edge_mask) != 0u;
+        __syncwarp();
+        return warp_or64(chg);
+    }
+    uint32_t prev[N];
+    P::unpack(sm.tm[(DOWN ? first - 1 : first + 1) * 32 + lane], prev);
 #pragma unroll 4
     for (int i = 0; i < count; ++i) {
         const int r = DOWN ? first + i : first - i;

@@ -639,10 +639,10 @@ __global__ void __launch_bounds__(kWarps * 32) engine_kernel(EngineArgs a) {
 // Job initialisation: every tile DIRTY; round 0 (double / unique) is the
 // virtual list of all tiles; the mutex stack holds every tile so that the
 // first pops come out in raster order (IWPP MP/src/globalQueue.cu:83-97,
-// initFillGlobalQueue).  After front passes the seed check has set the tile
-// states and listed the tiles to start from: the mutex stack and the first
-// round's read queue are that list, the async ring starts from it; the
-// passes' error and sweep count stand.
+// initFillGlobalQueue).  After the front stage (or a seed check alone) the
+// check has set the tile states and listed the tiles to start from: the
+// mutex stack and the first round's read queue are that list, the async
+// ring starts from it; the stage's error word and top-pixel count stand.
 __global__ void engine_init_kernel(EngineArgs a, int variant) {
     const unsigned stride = gridDim.x * blockDim.x;
     const bool seeded = a.init_list != nullptr;
@@ -688,6 +688,7 @@ __global__ void engine_init_kernel(EngineArgs a, int variant) {
         c->row_steps = 0ull;
         for (int i = 0; i < 5; ++i) c->phase[i] = 0ull;
         if (!a.front) c->top_pixels = 0ull;  // else the top-level stage's count stands
+        if (!a.front_gated) c->front_gate = a.front ? 1u : 0u;  // else the device's decision stands
     }
 }
 

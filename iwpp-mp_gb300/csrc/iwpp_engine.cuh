@@ -67,6 +67,7 @@ struct Ctrl {
     unsigned long long phase[5];  // cycles: queue read, fetch, processing, dump, queue write
     unsigned long long top_pixels;    // pixels the top-level stage labelled
     unsigned ninit;     // initial entries (every tile, or the seed list after front passes)
+    unsigned front_gate;  // front stage decided on the device: 1 run it, 0 leave the job to the engine
 };
 
 struct EngineArgs {
@@ -82,7 +83,8 @@ struct EngineArgs {
     int max_restarts;
     int solver;  // 0 automatic, 1 row sweeps, 2 passes
     int phantom;  // test hook: one unit of work that never arrives (every wait runs out)
-    int front;    // the front passes ran before this job's engine launch
+    int front;    // the front stage (or its seed check) ran before this job's engine launch
+    int front_gated;  // the device decided whether the stage ran (Ctrl::front_gate)
     // After front passes: the tiles to start from (ids) and their count (a
     // device counter); nullptr: every tile, in id order.  The tile states
     // were set by the seed check.
@@ -111,11 +113,11 @@ cudaError_t launch_fixed_point_check(const ImgDesc& d, unsigned long long* count
 // out[1] ids with a wrong count, out[2] the smallest such id.
 cudaError_t queue_selftest(const EngineArgs& a, int variant, int copies, unsigned* hist, unsigned long long* out,
                            int device, cudaStream_t s);
-// Whole-image sweep; 4-connected vertical sweeps use `scratch`
-// (sweep_scratch_bytes(d) bytes, nullable) for the single-pass form, whose
-// bounded waits set *err (nullable) to 3 when they run out.
+// Whole-image sweep; 4-connected vertical sweeps of tall uint8 / uint16
+// images use `scratch` (sweep_scratch_bytes(d) bytes, nullable) to split the
+// columns into segments.
 // `launches` (nullable) is incremented by the number of kernels launched.
 cudaError_t launch_sweep(const ImgDesc& d, int direction, cudaStream_t s, void* scratch = nullptr,
-                         int* launches = nullptr, unsigned* err = nullptr);
+                         int* launches = nullptr);
 size_t sweep_scratch_bytes(const ImgDesc& d);
 }  // namespace iwpp

@@ -109,6 +109,7 @@ constexpr int kXAhead = 2;
 
 template <int DT, bool FWD>
 __global__ void sweep_x_kernel(ImgDesc d) {
+    if (gated_off(d)) return;
     using P = Px<DT>;
     constexpr int TW = 32 * P::PPW;
     const int lane = threadIdx.x & 31;
@@ -158,6 +159,7 @@ __global__ void sweep_x_kernel(ImgDesc d) {
 // stored word by word.
 template <int DT, bool FWD>
 __global__ void sweep_x16_kernel(ImgDesc d) {
+    if (gated_off(d)) return;
     using P = Px<DT>;
     constexpr int WPL = 4;             // words per lane
     constexpr int N = WPL * P::PPW;    // pixels per lane
@@ -267,6 +269,7 @@ constexpr int kRing = 64, kGroup = 8;
 
 template <int DT, int CONN, bool DOWN>
 __global__ void __launch_bounds__(32) sweep_y_kernel(ImgDesc d) {
+    if (gated_off(d)) return;
     using P = Px<DT>;
     constexpr int TW = 32 * P::PPW;
     constexpr int N = P::PPW;
@@ -382,6 +385,7 @@ constexpr int kSegRows = 1024;
 template <int DT, bool DOWN, int MODE>
 __global__ void __launch_bounds__(32) sweep_y4n_kernel(ImgDesc d, uint32_t* seg_a, uint32_t* seg_b,
                                                        const uint32_t* seg_in) {
+    if (gated_off(d)) return;
     static_assert(DT == DT_U8 || DT == DT_U16, "two-byte lanes");
     using P = Px<DT>;
     constexpr int NR = kRingN, NG = kRingN / kGroup;
@@ -500,6 +504,7 @@ __global__ void __launch_bounds__(32) sweep_y4n_kernel(ImgDesc d, uint32_t* seg_
 template <bool DOWN, int MODE>
 __global__ void __launch_bounds__(32) sweep_y4i_kernel(ImgDesc d, uint32_t* seg_a, uint32_t* seg_b,
                                                        const uint32_t* seg_in) {
+    if (gated_off(d)) return;
     constexpr int NG = kRing / kGroup;
     __shared__ __align__(16) uint32_t ring_m[kRing][32];
     __shared__ __align__(16) uint32_t ring_k[kRing][32];
@@ -606,187 +611,15 @@ __global__ void sweep_y_carry_kernel(int nseg, int slots, const uint32_t* seg_a,
     }
 }
 
-// ---------------------------------------------- single-pass Y sweeps
-// 4-connected vertical sweep reading each plane once.  The image is cut into
-// units of kLbRows rows x 512 bytes; a CTA of 128 threads takes one unit,
-// a thread one 4-byte column word (4 / 2 / 1 columns, updated together by
-// byte / half-word SIMD), all of the unit's rows held in registers.  The
-// update of a column over a unit is the clamp map x -> max(min(x, B), A)
-// (A: the unit's last value when nothing enters, B: its least mask), and the
-// units of a column chain by decoupled look-back, as in a single-pass prefix
-// scan: a unit publishes its map (AGG), then walks back over its
-// predecessors composing their maps until one has published the value
-// leaving it (INCL), publishes its own leaving value and only then applies
-// the entering value to its rows and stores the words that rose.  Units are
-// taken in ticket order (row band by row band), so every unit waited on
-// holds a ticket, is resident or done, and publishes: the waits end.  Each
-// is still bounded; one that runs out takes nothing as the entering value
-// (a partial, still valid update) and sets *err.
-constexpr int kLbRows = 32;
-constexpr int kLbThreads = 128;  // 512 bytes: one 4-byte column word per thread
-constexpr long long kLbTimeoutNs = 4000000000ll;
-enum : unsigned { LB_NONE = 0u, LB_AGG = 1u, LB_INCL = 2u };
-
-template <int DT>
-__device__ __forceinline__ uint32_t lb_max(uint32_t a, uint32_t b) {
-    if (DT == DT_U8) return __vmaxu4(a, b);
-    if (DT == DT_U16) return __vmaxu2(a, b);
-    return (uint32_t)max((int)a, (int)b);
-}
-template <int DT>
-__device__ __forceinline__ uint32_t lb_min(uint32_t a, uint32_t b) {
-    if (DT == DT_U8) return __vminu4(a, b);
-    if (DT == DT_U16) return __vminu2(a, b);
-    return (uint32_t)min((int)a, (int)b);
-}
-
-struct LbArgs {
-    ImgDesc d;
-    int groups;        // 512-byte column groups across the image
-    unsigned* ticket;  // units handed out
-    unsigned* flag;    // per unit: LB_NONE / LB_AGG / LB_INCL
-    uint32_t* agg_a;   // per unit and column word: the map's A
-    uint32_t* agg_b;   //                                  B
-    uint32_t* incl;    //                            the value leaving the unit
-    unsigned* err;     // nullable: set to 3 when a wait ran out
-};
-
-template <int DT, bool DOWN>
-__global__ void __launch_bounds__(kLbThreads) sweep_y_lb_kernel(LbArgs a) {
-    using P = Px<DT>;
-    constexpr uint32_t MAXW = DT == DT_I32 ? 0x7fffffffu : 0xffffffffu;
-    __shared__ unsigned s_unit;
-    const ImgDesc& d = a.d;
-    const int t = threadIdx.x;
-    if (t == 0) s_unit = atomicAdd(a.ticket, 1u);
-    __syncthreads();
-    const unsigned u = s_unit;
-    const int j = (int)(u / (unsigned)a.groups), g = (int)(u - (unsigned)j * (unsigned)a.groups);
-    const long long row_bytes = (long long)d.W * P::BPP;
-    const long long b0 = (long long)g * 512 + t * 4;
-    const int npx = b0 < row_bytes ? (int)min((long long)P::PPW, (row_bytes - b0) / P::BPP) : 0;
-    const int i0 = j * kLbRows, rows = min(kLbRows, d.H - i0);
-    auto row_y = [&](int r) { return DOWN ? i0 + r : d.H - 1 - i0 - r; };
-    // the unit's words (rows past the image: the identity, m = least, k = largest)
-    uint32_t m[kLbRows], k[kLbRows];
-#pragma unroll
-    for (int r = 0; r < kLbRows; ++r) {
-        m[r] = P::MINW;
-        k[r] = MAXW;
-        if (r < rows && npx > 0) {
-            const size_t y = (size_t)row_y(r);
-            m[r] = load_word_plain<DT>(d.marker + y * d.pitch_m + b0, npx, true);
-            k[r] = load_word_plain<DT>(d.mask + y * d.pitch_k + b0, npx, false);
-        }
-    }
-    // the unit's map
-    uint32_t A = P::MINW, B = MAXW;
-#pragma unroll
-    for (int r = 0; r < kLbRows; ++r) {
-        A = lb_max<DT>(m[r], lb_min<DT>(A, k[r]));
-        B = lb_min<DT>(B, k[r]);
-    }
-    const size_t slot = (size_t)u * kLbThreads + t;
-    uint32_t carry = P::MINW;
-    if (j > 0) {
-        a.agg_a[slot] = A;
-        a.agg_b[slot] = B;
-        __threadfence();
-        __syncthreads();
-        if (t == 0) st_release(&a.flag[u], LB_AGG);
-        // look back: the composed map of the units between, then the value
-        // leaving the nearest unit that has published it
-        uint32_t gA = P::MINW, gB = MAXW;  // identity
-        const long long t0 = globaltimer_ns();
-        bool gave_up = false;
-        for (int jj = j - 1; jj >= 0; --jj) {
-            const unsigned pu = (unsigned)jj * (unsigned)a.groups + (unsigned)g;
-            unsigned f;
-            unsigned spins = 0;
-            while ((f = ld_acquire(&a.flag[pu])) == LB_NONE) {
-                __nanosleep(64);
-                if ((++spins & 63u) == 0u && globaltimer_ns() - t0 > kLbTimeoutNs) {
-                    gave_up = true;
-                    break;
-                }
-            }
-            if (gave_up) {
-                if (a.err) atomicExch(a.err, 3u);
-                carry = lb_max<DT>(lb_min<DT>(P::MINW, gB), gA);
-                break;
-            }
-            const size_t ps = (size_t)pu * kLbThreads + t;
-            if (f == LB_INCL) {
-                carry = lb_max<DT>(lb_min<DT>(__ldcg(&a.incl[ps]), gB), gA);
-                break;
-            }
-            // g o f_jj: A = max(min(A_f, B_g), A_g), B = min(B_f, B_g)
-            const uint32_t fA = __ldcg(&a.agg_a[ps]), fB = __ldcg(&a.agg_b[ps]);
-            gA = lb_max<DT>(lb_min<DT>(fA, gB), gA);
-            gB = lb_min<DT>(fB, gB);
-        }
-    }
-    a.incl[slot] = lb_max<DT>(lb_min<DT>(carry, B), A);
-    __threadfence();
-    __syncthreads();
-    if (t == 0) st_release(&a.flag[u], LB_INCL);
-    // the rows from the entering value; the words that rose are stored
-    if (npx > 0) {
-        uint32_t prev = carry;
-#pragma unroll
-        for (int r = 0; r < kLbRows; ++r) {
-            if (r < rows) {
-                const uint32_t v = lb_max<DT>(m[r], lb_min<DT>(prev, k[r]));
-                if (v != m[r]) store_word_plain<DT>(d.marker + (size_t)row_y(r) * d.pitch_m + b0, npx, v);
-                prev = v;
-            }
-        }
-    }
-}
-
-static void lb_dims(const ImgDesc& d, long long* groups, long long* units) {
-    const int bpp = d.dtype == DT_U8 ? 1 : d.dtype == DT_U16 ? 2 : 4;
-    *groups = ((long long)d.W * bpp + 511) / 512;
-    *units = *groups * ((d.H + kLbRows - 1) / kLbRows);
-}
-
-static size_t lb_al(size_t v) { return (v + 255) / 256 * 256; }
-
-// The 4-connected vertical sweeps take the single-pass form (its flags and
-// maps in the scratch); other sweeps need none.
+// int32 is not segmented: at four bytes a pixel the two extra plane reads
+// cost more than the parallelism gains (its strips already give 512 warps
+// on a 16384-wide image).
 size_t sweep_scratch_bytes(const ImgDesc& d) {
-    if (d.conn != 4 || d.W == 0 || d.H == 0) return 0;
-    long long groups, units;
-    lb_dims(d, &groups, &units);
-    return lb_al(4) + lb_al((size_t)units * 4) + 3 * lb_al((size_t)units * kLbThreads * 4);
-}
-
-template <int DT>
-static cudaError_t launch_sweep_y_lb(const ImgDesc& d, bool down, void* scratch, unsigned* err, cudaStream_t s) {
-    long long groups, units;
-    lb_dims(d, &groups, &units);
-    LbArgs a{};
-    a.d = d;
-    a.groups = (int)groups;
-    char* p = static_cast<char*>(scratch);
-    a.ticket = reinterpret_cast<unsigned*>(p);
-    p += lb_al(4);
-    a.flag = reinterpret_cast<unsigned*>(p);
-    p += lb_al((size_t)units * 4);
-    a.agg_a = reinterpret_cast<uint32_t*>(p);
-    p += lb_al((size_t)units * kLbThreads * 4);
-    a.agg_b = reinterpret_cast<uint32_t*>(p);
-    p += lb_al((size_t)units * kLbThreads * 4);
-    a.incl = reinterpret_cast<uint32_t*>(p);
-    a.err = err;
-    // the ticket and the flags (adjacent) start at zero
-    cudaError_t e = cudaMemsetAsync(scratch, 0, lb_al(4) + (size_t)units * 4, s);
-    if (e != cudaSuccess) return e;
-    if (down)
-        sweep_y_lb_kernel<DT, true><<<(unsigned)units, kLbThreads, 0, s>>>(a);
-    else
-        sweep_y_lb_kernel<DT, false><<<(unsigned)units, kLbThreads, 0, s>>>(a);
-    return cudaGetLastError();
+    if (d.conn != 4 || d.dtype == DT_I32 || d.H <= 2 * kSegRows) return 0;
+    const long long strips = d.dtype == DT_I32 ? ((long long)d.W + 31) / 32
+                                               : ((long long)d.W * (d.dtype == DT_U8 ? 1 : 2) + 63) / 64;
+    const long long nseg = (d.H + kSegRows - 1) / kSegRows;
+    return (size_t)(3 * nseg * strips * 32 * 4);
 }
 
 // ------------------------------------------------------------ host side
@@ -825,10 +658,8 @@ cudaError_t launch_clip(const ImgDesc& d, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-constexpr bool kUseLookBack = true;
-
 template <int DT>
-static int launch_sweep_t(const ImgDesc& d, int direction, cudaStream_t s, void* scratch, unsigned* err) {
+static int launch_sweep_t(const ImgDesc& d, int direction, cudaStream_t s, void* scratch) {
     using P = Px<DT>;
     constexpr int TW = 32 * P::PPW;
     if (direction == 0 || direction == 2) {
@@ -856,9 +687,6 @@ static int launch_sweep_t(const ImgDesc& d, int direction, cudaStream_t s, void*
                 sweep_y_kernel<DT, 8, true><<<blocks, 32, 0, s>>>(d);
             else
                 sweep_y_kernel<DT, 8, false><<<blocks, 32, 0, s>>>(d);
-        } else if (scratch && kUseLookBack) {
-            if (launch_sweep_y_lb<DT>(d, down, scratch, err, s) != cudaSuccess) return 0;
-            return 1;
         } else if (DT == DT_I32) {
             const unsigned nblocks = (unsigned)((d.W + 31) / 32);
             if (scratch && sweep_scratch_bytes(d) > 0) {
@@ -914,16 +742,15 @@ static int launch_sweep_t(const ImgDesc& d, int direction, cudaStream_t s, void*
     }
 }
 
-cudaError_t launch_sweep(const ImgDesc& d, int direction, cudaStream_t s, void* scratch, int* launches,
-                         unsigned* err) {
+cudaError_t launch_sweep(const ImgDesc& d, int direction, cudaStream_t s, void* scratch, int* launches) {
     if (d.W == 0 || d.H == 0) return cudaSuccess;
     int n;
     if (d.dtype == DT_U8)
-        n = launch_sweep_t<DT_U8>(d, direction, s, scratch, err);
+        n = launch_sweep_t<DT_U8>(d, direction, s, scratch);
     else if (d.dtype == DT_U16)
-        n = launch_sweep_t<DT_U16>(d, direction, s, scratch, err);
+        n = launch_sweep_t<DT_U16>(d, direction, s, scratch);
     else
-        n = launch_sweep_t<DT_I32>(d, direction, s, scratch, err);
+        n = launch_sweep_t<DT_I32>(d, direction, s, scratch);
     if (launches) *launches += n;
     return cudaGetLastError();
 }

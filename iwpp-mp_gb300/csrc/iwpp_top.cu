@@ -65,6 +65,9 @@ struct TopArgs {
     int edge_stride;         // 128 + 2 * tw
     int* tn;                 // per tile: its top-level pixels
     unsigned* tlist;         // per tile: kTopListCap entries, pixel | slot << 16 (slot 0xff: none)
+    unsigned* ncount;        // [0]: tiles with a saved list, [1]: tiles to label again
+    unsigned* listed;        // the tiles with a saved list
+    unsigned* relabel;       // the tiles with more top-level pixels than a list holds
     int aligned16;           // mask rows start on 16-byte boundaries
     unsigned long long* top_pixels;  // the job's count of pixels labelled
 };
@@ -96,15 +99,16 @@ __device__ __forceinline__ void g_union(int* parent, int a, int b) {
     }
 }
 
-__device__ __forceinline__ int s_find(int* parent, int x) {
+// The same in shared memory, over a tile's pixel indices (16 bits).
+__device__ __forceinline__ int s_find(unsigned short* parent, int x) {
     for (;;) {
-        const int p = *(volatile int*)&parent[x];
+        const int p = *(volatile unsigned short*)&parent[x];
         if (p == x) return x;
         x = p;
     }
 }
 
-__device__ __forceinline__ void s_union(int* parent, int a, int b) {
+__device__ __forceinline__ void s_union(unsigned short* parent, int a, int b) {
     for (;;) {
         a = s_find(parent, a);
         b = s_find(parent, b);
@@ -114,7 +118,7 @@ __device__ __forceinline__ void s_union(int* parent, int a, int b) {
             a = b;
             b = t;
         }
-        const int old = atomicCAS(&parent[a], a, b);
+        const int old = atomicCAS(&parent[a], (unsigned short)a, (unsigned short)b);
         if (old == a) return;
         a = old;
     }
@@ -135,19 +139,12 @@ __device__ __forceinline__ uint32_t word_max_key(uint32_t w) {
     }
 }
 
-// Per-lane running maximum of a word into `acc` (byte / half-word lanes
-// for uint8 / uint16, signed for int32).
-template <int DT>
-__device__ __forceinline__ uint32_t word_max(uint32_t acc, uint32_t w) {
-    if (DT == DT_U8) return __vmaxu4(acc, w);
-    if (DT == DT_U16) return __vmaxu2(acc, w);
-    return (uint32_t)max((int)acc, (int)w);
-}
 
 // One warp per tile; with 16-byte rows each lane reads 16 bytes of a row
 // (8 lanes a row, 4 rows per step), else one word of each row.
 template <int DT>
 __global__ void top_max_kernel(TopArgs a) {
+    if (gated_off(a.d)) return;
     using P = Px<DT>;
     const int lane = threadIdx.x & 31;
     const long long G = (long long)a.tx_n * a.ty_n;
@@ -198,13 +195,15 @@ __global__ void top_max_kernel(TopArgs a) {
 }
 
 // ------------------------------------------------- 2 / 5. local labelling
-// Shared memory of a CTA working on one tile: the union-find parents of the
-// tile's pixels (-1: not at the top level), the list of its top-level
-// pixels, the node slot of each root and per slot its component's value.
+// Shared memory of a CTA working on one tile: which pixels are at the top
+// level (per row, word j bit l: pixel l * PPW + j), the union-find parents
+// of those pixels (the others' entries are not written), the list of them,
+// the node slot of each root and per slot its component's value.
 template <int DT>
 struct TopSmem {
     static constexpr int NPX = kTopRows * 32 * Px<DT>::PPW;
-    int parent[NPX];
+    unsigned topbits[kTopRows][Px<DT>::PPW];
+    unsigned short parent[NPX];
     unsigned short list[NPX];
     signed char slot[NPX];
     unsigned sval[kTopSlots];  // local: largest capped marker key; apply: the component's
@@ -217,10 +216,18 @@ struct TopSmem {
 // i * kTopThreads is tile row w / 32, lane word w % 32.
 constexpr int kTopWpt = kTopRows * 32 / kTopThreads;
 
+// Pixel p of the tile is at the top level.
+template <int DT>
+__device__ __forceinline__ bool is_top(const TopSmem<DT>& sm, int p) {
+    constexpr int TW = 32 * Px<DT>::PPW;
+    const int r = p / TW, c = p - r * TW;
+    return (sm.topbits[r][c % Px<DT>::PPW] >> (c / Px<DT>::PPW)) & 1u;
+}
+
 // The tile's top-level pixels labelled: sm.list[0, sm.nlist) holds them,
-// sm.parent[p] the least pixel index of p's component (-1 for the other
-// pixels).  Returns the thread's top-level flags: bit i * PPW + j for pixel j
-// of its word i.  All threads of the CTA.
+// sm.parent[p] the least pixel index of p's component (top-level p only).
+// Returns the thread's top-level flags: bit i * PPW + j for pixel j of its
+// word i.  All threads of the CTA.
 template <int DT>
 __device__ unsigned label_tile(const TopArgs& a, int tx, int ty, unsigned tkey, TopSmem<DT>& sm) {
     using P = Px<DT>;
@@ -250,8 +257,13 @@ __device__ unsigned label_tile(const TopArgs& a, int tx, int ty, unsigned tkey, 
         for (int j = 0; j < P::PPW; ++j) {
             const int p = r * TW + c0 + j;
             const bool top = y0 + r < d.H && x0 + c0 + j < d.W && top_key<DT>(k[j]) >= tkey;
-            sm.parent[p] = top ? p : -1;
-            if (top) bits |= 1u << (i * P::PPW + j);
+            if (top) {
+                sm.parent[p] = (unsigned short)p;
+                bits |= 1u << (i * P::PPW + j);
+            }
+            // the warp holds the whole row r: one ballot per pixel position
+            const unsigned row_bits = __ballot_sync(FULL, top);
+            if (lane == j) sm.topbits[r][j] = row_bits;
         }
     }
     // the list: each thread's place by a CTA-wide exclusive scan of counts
@@ -278,12 +290,12 @@ __device__ unsigned label_tile(const TopArgs& a, int tx, int ty, unsigned tkey, 
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
         const int p = sm.list[e];
         const int r = p / TW, c = p - r * TW;
-        if (c > 0 && sm.parent[p - 1] >= 0) s_union(sm.parent, p, p - 1);
+        if (c > 0 && is_top<DT>(sm, p - 1)) s_union(sm.parent, p, p - 1);
         if (r > 0) {
-            if (sm.parent[p - TW] >= 0) s_union(sm.parent, p, p - TW);
+            if (is_top<DT>(sm, p - TW)) s_union(sm.parent, p, p - TW);
             if (a.conn == 8) {
-                if (c > 0 && sm.parent[p - TW - 1] >= 0) s_union(sm.parent, p, p - TW - 1);
-                if (c + 1 < TW && sm.parent[p - TW + 1] >= 0) s_union(sm.parent, p, p - TW + 1);
+                if (c > 0 && is_top<DT>(sm, p - TW - 1)) s_union(sm.parent, p, p - TW - 1);
+                if (c + 1 < TW && is_top<DT>(sm, p - TW + 1)) s_union(sm.parent, p, p - TW + 1);
             }
         }
     }
@@ -315,7 +327,8 @@ __device__ __forceinline__ void load_top_words(const ImgDesc& d, int tx, int ty,
 }
 
 template <int DT>
-__global__ void __launch_bounds__(kTopThreads) top_local_kernel(TopArgs a) {
+__global__ void __launch_bounds__(kTopThreads, 4) top_local_kernel(TopArgs a) {
+    if (gated_off(a.d)) return;
     using P = Px<DT>;
     constexpr int TW = 32 * P::PPW;
     extern __shared__ __align__(16) unsigned char top_smem[];
@@ -385,8 +398,7 @@ __global__ void __launch_bounds__(kTopThreads) top_local_kernel(TopArgs a) {
             else if (i < 128) p = (i - 64) * TW + TW - 1;    // right column
             else if (i < 128 + TW) p = i - 128;              // top row
             else p = (kTopRows - 1) * TW + (i - 128 - TW);   // bottom row
-            const int root = sm.parent[p];
-            e[i] = root < 0 ? (signed char)-1 : sm.slot[root];
+            e[i] = is_top<DT>(sm, p) ? sm.slot[sm.parent[p]] : (signed char)-1;
         }
         // the (pixel, slot) list for the apply step, when it fits
         if (n <= kTopListCap)
@@ -401,6 +413,10 @@ __global__ void __launch_bounds__(kTopThreads) top_local_kernel(TopArgs a) {
             a.ns[t] = ns;
             a.tn[t] = n;
             atomicAdd(a.top_pixels, (unsigned long long)n);
+            if (n <= kTopListCap)
+                a.listed[atomicAdd(&a.ncount[0], 1u)] = (unsigned)t;
+            else
+                a.relabel[atomicAdd(&a.ncount[1], 1u)] = (unsigned)t;
         }
         __syncthreads();
     }
@@ -411,6 +427,7 @@ __global__ void __launch_bounds__(kTopThreads) top_local_kernel(TopArgs a) {
 // (and the corners for 8-connectivity); both tiles must hold top-level
 // pixels (their edge slots are written).
 __global__ void top_union_kernel(TopArgs a) {
+    if (gated_off(a.d)) return;
     const int TW = a.tw;
     const long long G = (long long)a.tx_n * a.ty_n;
     const int per = 2 * kTopRows + 2 * TW + 2;  // work items per tile
@@ -478,6 +495,7 @@ __global__ void top_union_kernel(TopArgs a) {
 
 // ---------------------------------------------------------- 4. flatten
 __global__ void top_flatten_kernel(TopArgs a) {
+    if (gated_off(a.d)) return;
     const long long total = (long long)a.tx_n * a.ty_n * kTopSlots;
     const unsigned tkey = *(const volatile unsigned*)a.thr_key;
     for (long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x; node < total;
@@ -496,18 +514,17 @@ __global__ void top_flatten_kernel(TopArgs a) {
 // point at their roots after the flatten step.
 template <int DT>
 __global__ void top_apply_list_kernel(TopArgs a) {
+    if (gated_off(a.d)) return;
     using P = Px<DT>;
     constexpr int TW = 32 * P::PPW;
     const int lane = threadIdx.x & 31;
     const ImgDesc& d = a.d;
-    const unsigned tkey = *(const volatile unsigned*)a.thr_key;
-    const long long G = (long long)a.tx_n * a.ty_n;
+    const long long count = *(const volatile unsigned*)&a.ncount[0];
     const long long wg = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long t = wg; t < G; t += nw) {
-        if (a.tmax[t] < tkey) continue;
+    for (long long i = wg; i < count; i += nw) {
+        const long long t = a.listed[i];
         const int n = a.tn[t];
-        if (n > kTopListCap) continue;
         const int ty = (int)(t / a.tx_n), tx = (int)(t - (long long)ty * a.tx_n);
         for (int e = lane; e < n; e += 32) {
             const unsigned u = a.tlist[t * kTopListCap + e];
@@ -524,16 +541,17 @@ __global__ void top_apply_list_kernel(TopArgs a) {
 // Tiles with more top-level pixels than the list holds: a CTA per tile
 // labels the tile again.
 template <int DT>
-__global__ void __launch_bounds__(kTopThreads) top_apply_label_kernel(TopArgs a) {
+__global__ void __launch_bounds__(kTopThreads, 4) top_apply_label_kernel(TopArgs a) {
+    if (gated_off(a.d)) return;
     using P = Px<DT>;
     constexpr int TW = 32 * P::PPW;
     extern __shared__ __align__(16) unsigned char top_smem[];
     TopSmem<DT>& sm = *reinterpret_cast<TopSmem<DT>*>(top_smem);
     const ImgDesc& d = a.d;
     const unsigned tkey = *(const volatile unsigned*)a.thr_key;
-    const long long G = (long long)a.tx_n * a.ty_n;
-    for (long long t = blockIdx.x; t < G; t += gridDim.x) {
-        if (a.tmax[t] < tkey || a.tn[t] <= kTopListCap) continue;
+    const long long count = *(const volatile unsigned*)&a.ncount[1];
+    for (long long i = blockIdx.x; i < count; i += gridDim.x) {
+        const long long t = a.relabel[i];
         const int ty = (int)(t / a.tx_n), tx = (int)(t - (long long)ty * a.tx_n);
         const unsigned bits = label_tile<DT>(a, tx, ty, tkey, sm);
         const int n = sm.nlist;
@@ -617,6 +635,7 @@ __device__ __forceinline__ uint32_t seed_px(const ImgDesc& d, int y, int x) {
 
 template <int DT>
 __global__ void seed_kernel(const ImgDesc d, unsigned* state, unsigned* list, unsigned* nlist) {
+    if (gated_off(d)) return;
     using P = Px<DT>;
     constexpr int N = P::PPW;
     constexpr int TW = 32 * N;
@@ -687,6 +706,150 @@ __global__ void seed_kernel(const ImgDesc d, unsigned* state, unsigned* list, un
     }
 }
 
+// The same check with 16-byte lanes: a warp covers four engine tiles side by
+// side (8 lanes each, 512 bytes of a row), the words of a lane updated with
+// byte / half-word SIMD, the side neighbours of a word's pixels by funnel
+// shifts of the adjacent words, and rows loaded kSeedAhead ahead into a
+// register ring.  Rows must start on 16-byte boundaries (both planes).
+constexpr int kSeedAhead = 2;
+constexpr int kSeedThreads = 128;
+
+// 16 bytes of row y from byte b0 (pixels past the row or outside the image:
+// the least value).
+template <int DT>
+__device__ __forceinline__ uint4 seed_load16(const ImgDesc& d, const unsigned char* base, long long pitch, int y,
+                                             long long b0, long long row_bytes) {
+    using P = Px<DT>;
+    uint4 v = make_uint4(P::MINW, P::MINW, P::MINW, P::MINW);
+    if (y < 0 || y >= d.H || b0 >= row_bytes) return v;
+    const unsigned char* p = base + (size_t)y * pitch + b0;
+    if (b0 + 16 <= row_bytes) return __ldg(reinterpret_cast<const uint4*>(p));
+    uint32_t w[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const long long b = b0 + 4 * i;
+        w[i] = b < row_bytes ? load_word_plain<DT>(p + 4 * i, (int)((row_bytes - b) / P::BPP), false) : P::MINW;
+    }
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+template <int DT>
+__global__ void __launch_bounds__(kSeedThreads, 4)
+    seed16_kernel(const ImgDesc d, unsigned* state, unsigned* list, unsigned* nlist) {
+    if (gated_off(d)) return;
+    using P = Px<DT>;
+    constexpr int BITS = 8 * P::BPP;  // bits per pixel
+    constexpr int TW = 32 * P::PPW;   // pixels per engine tile row
+    const int lane = threadIdx.x & 31;
+    const int q = lane >> 3;          // this lane's tile of the four
+    const int gx_n = (d.tiles_x + 3) / 4;
+    const long long units = (long long)gx_n * d.tiles_y;
+    const long long wg = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int TH = d.tile_rows;
+    const long long row_bytes = (long long)d.W * P::BPP;
+    for (long long unit = wg; unit < units; unit += nw) {
+        const int ty = (int)(unit / gx_n), gx = (int)(unit - (long long)ty * gx_n);
+        const int y0 = ty * TH, rows = min(TH, d.H - y0);
+        const long long b0 = (long long)gx * 512 + lane * 16;
+        const int xl = gx * 4 * TW - 1, xr = (gx + 1) * 4 * TW;  // halo columns
+        auto halo = [&](int y) -> uint32_t {
+            if (lane == 0) return seed_px<DT>(d, y, xl);
+            if (lane == 31) return seed_px<DT>(d, y, xr);
+            return P::MINPX;
+        };
+        // window: marker rows r - 1, r (words), mask row r, halo pixels
+        uint4 mu = seed_load16<DT>(d, d.marker, d.pitch_m, y0 - 1, b0, row_bytes);
+        uint4 mc = seed_load16<DT>(d, d.marker, d.pitch_m, y0, b0, row_bytes);
+        uint4 kc = seed_load16<DT>(d, d.mask, d.pitch_k, y0, b0, row_bytes);
+        uint32_t hu = halo(y0 - 1), hc = halo(y0);
+        // ring slot i holds marker / mask / halo of row r + 1 + i
+        uint4 rm[kSeedAhead], rk[kSeedAhead];
+        uint32_t rh[kSeedAhead];
+#pragma unroll
+        for (int i = 0; i < kSeedAhead; ++i) {
+            const int y = y0 + 1 + i;
+            rm[i] = seed_load16<DT>(d, d.marker, d.pitch_m, y, b0, row_bytes);
+            rk[i] = i + 1 < rows ? seed_load16<DT>(d, d.mask, d.pitch_k, y, b0, row_bytes)
+                                 : make_uint4(P::MINW, P::MINW, P::MINW, P::MINW);
+            rh[i] = halo(y);
+        }
+        bool mine = false;
+        for (int r0 = 0; r0 < rows; r0 += kSeedAhead) {
+#pragma unroll
+            for (int i = 0; i < kSeedAhead; ++i) {
+                const int r = r0 + i;
+                if (r >= rows) break;  // warp-uniform
+                const uint4 md = rm[i], kn = rk[i];
+                const uint32_t hd = rh[i];
+                {
+                    const int y = y0 + r + 1 + kSeedAhead;
+                    rm[i] = seed_load16<DT>(d, d.marker, d.pitch_m, y, b0, row_bytes);
+                    rk[i] = r + 1 + kSeedAhead < rows ? seed_load16<DT>(d, d.mask, d.pitch_k, y, b0, row_bytes)
+                                                     : make_uint4(P::MINW, P::MINW, P::MINW, P::MINW);
+                    rh[i] = halo(y);
+                }
+                const uint32_t U[4] = {mu.x, mu.y, mu.z, mu.w}, C[4] = {mc.x, mc.y, mc.z, mc.w};
+                const uint32_t Dn[4] = {md.x, md.y, md.z, md.w}, K[4] = {kc.x, kc.y, kc.z, kc.w};
+                // what a column offers its side neighbours: itself, or with
+                // 8-connectivity the largest of its three rows
+                uint32_t V[4], S[4];
+#pragma unroll
+                for (int w = 0; w < 4; ++w) {
+                    V[w] = word_max<DT>(U[w], Dn[w]);
+                    S[w] = d.conn == 8 ? word_max<DT>(V[w], C[w]) : C[w];
+                }
+                const uint32_t hs = d.conn == 8 ? P::mx(P::mx(hu, hc), hd) : hc;
+                uint32_t left = __shfl_up_sync(FULL, S[3], 1), right = __shfl_down_sync(FULL, S[0], 1);
+                if (lane == 0) left = BITS == 32 ? hs : hs << (32 - BITS);
+                if (lane == 31) right = hs;
+#pragma unroll
+                for (int w = 0; w < 4; ++w) {
+                    // clamped funnel shifts: a shift of 32 (int32) yields the
+                    // adjacent word itself
+                    const uint32_t lw = __funnelshift_lc(w == 0 ? left : S[w - 1], S[w], BITS);
+                    const uint32_t rw = __funnelshift_rc(S[w], w == 3 ? right : S[w + 1], BITS);
+                    const uint32_t best = word_max<DT>(V[w], word_max<DT>(lw, rw));
+                    mine |= word_any_gt<DT>(word_min<DT>(best, K[w]), C[w]);
+                }
+                mu = mc;
+                mc = md;
+                kc = kn;
+                hu = hc;
+                hc = hd;
+            }
+        }
+        // a tile is bad when one of its 8 lanes saw a pixel to raise
+        const unsigned bad = __ballot_sync(FULL, mine);
+        const int tx = gx * 4 + q;
+        if ((lane & 7) == 0 && tx < d.tiles_x) {
+            const bool b = ((bad >> (q * 8)) & 0xffu) != 0u;
+            const unsigned g = (unsigned)d.tile_base + (unsigned)(ty * d.tiles_x + tx);
+            state[g] = b ? (ST_DIRTY | ST_SIDES) : 0u;
+            if (b) list[atomicAdd(nlist, 1u)] = g;
+        }
+    }
+}
+
+// --------------------------------------------------- the device decision
+// Decides, from the seed check over the untouched images, whether the job
+// takes the front stage: a small initial front (some tiles, but fewer than
+// one in kFrontDecideRatio, holding a pixel a neighbour can raise: a few
+// sparse seeds) propagates over long paths, one dependent tile visit per tile for
+// the engine alone, which the labelling and the whole-image passes cover
+// in a fixed number of sweeps; a large front (h-dome markers, dense seeds)
+// is short-range work the engine does faster alone.  With the stage the
+// seed list is emptied for the check after the passes; without it the list
+// of this check seeds the engine.
+constexpr unsigned kFrontDecideRatio = 64;
+
+__global__ void front_decide_kernel(unsigned* gate, unsigned* count, unsigned G) {
+    const unsigned n = *(volatile unsigned*)count;
+    const unsigned front = n > 0u && (unsigned long long)n * kFrontDecideRatio < (unsigned long long)G ? 1u : 0u;
+    *gate = front;
+    if (front) *count = 0u;
+}
+
 // ------------------------------------------------------------------ host
 static size_t tal(size_t v) { return (v + 255) / 256 * 256; }
 
@@ -702,7 +865,7 @@ size_t top_scratch_bytes(const ImgDesc& d) {
     top_dims(d, &tx_n, &ty_n, &tw);
     const size_t G = (size_t)tx_n * ty_n, nodes = G * kTopSlots;
     return tal(256) + tal(G * 4) + tal(G * 4) + tal(nodes * 4) + tal(nodes * 4) + tal(nodes * 2) +
-           tal(G * (128 + 2 * (size_t)tw)) + tal(G * 4) + tal(G * kTopListCap * 4);
+           tal(G * (128 + 2 * (size_t)tw)) + tal(G * 4) + tal(G * kTopListCap * 4) + tal(8) + 2 * tal(G * 4);
 }
 
 template <int DT>
@@ -757,11 +920,18 @@ cudaError_t launch_top(const ImgDesc& d, void* scratch, unsigned long long* top_
     a.tn = reinterpret_cast<int*>(p);
     p += tal(G * 4);
     a.tlist = reinterpret_cast<unsigned*>(p);
+    p += tal(G * kTopListCap * 4);
+    a.ncount = reinterpret_cast<unsigned*>(p);
+    p += tal(8);
+    a.listed = reinterpret_cast<unsigned*>(p);
+    p += tal(G * 4);
+    a.relabel = reinterpret_cast<unsigned*>(p);
     a.aligned16 = (reinterpret_cast<uintptr_t>(d.mask) & 15u) == 0u && (d.pitch_k & 15) == 0;
     a.top_pixels = top_pixels;
     int sms = 0;
     cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaMemsetAsync(a.thr_key, 0, sizeof(unsigned), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.ncount, 0, 2 * sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
     if (d.dtype == DT_U8)
         e = launch_top_t<DT_U8>(a, sms, s);
@@ -773,9 +943,32 @@ cudaError_t launch_top(const ImgDesc& d, void* scratch, unsigned long long* top_
     return e;
 }
 
+cudaError_t launch_front_decide(unsigned* gate, unsigned* count, unsigned G, cudaStream_t s, int* launches) {
+    front_decide_kernel<<<1, 1, 0, s>>>(gate, count, G);
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_seed(const ImgDesc& d, unsigned* state, unsigned* list, unsigned* nlist, cudaStream_t s,
                         int* launches) {
     if (d.W == 0 || d.H == 0) return cudaSuccess;
+    const bool aligned16 =
+        ((reinterpret_cast<uintptr_t>(d.marker) | reinterpret_cast<uintptr_t>(d.mask)) & 15u) == 0u &&
+        ((d.pitch_m | d.pitch_k) & 15) == 0;
+    if (aligned16) {
+        const long long units = (long long)((d.tiles_x + 3) / 4) * d.tiles_y;
+        long long blocks = (units * 32 + kSeedThreads - 1) / kSeedThreads;
+        if (blocks > 152ll * 32) blocks = 152ll * 32;
+        if (blocks < 1) blocks = 1;
+        if (d.dtype == DT_U8)
+            seed16_kernel<DT_U8><<<(unsigned)blocks, kSeedThreads, 0, s>>>(d, state, list, nlist);
+        else if (d.dtype == DT_U16)
+            seed16_kernel<DT_U16><<<(unsigned)blocks, kSeedThreads, 0, s>>>(d, state, list, nlist);
+        else
+            seed16_kernel<DT_I32><<<(unsigned)blocks, kSeedThreads, 0, s>>>(d, state, list, nlist);
+        if (launches) ++*launches;
+        return cudaGetLastError();
+    }
     const long long tiles = (long long)d.tiles_x * d.tiles_y;
     long long blocks = (tiles * 32 + 255) / 256;
     if (blocks > 152ll * 16) blocks = 152ll * 16;

@@ -17,8 +17,13 @@ cudaError_t launch_top(const ImgDesc& d, void* scratch, unsigned long long* top_
                        int* launches);
 // Marks every engine tile of image d (tile height d.tile_rows) that holds a
 // pixel a neighbour could raise DIRTY in `state` (others 0) and appends its
-// global id to `list`, counting in *nlist.
+// global id to `list`, counting in *nlist.  With d.gate set it does nothing
+// while *d.gate is 0 (so do the top-level stage and the sweeps).
 cudaError_t launch_seed(const ImgDesc& d, unsigned* state, unsigned* list, unsigned* nlist, cudaStream_t s,
                         int* launches);
+// After a seed check over a job's G tiles (its count in *count): *gate = 1
+// and *count = 0 when the initial front is small enough for the front stage
+// to pay, else *gate = 0 (the list stands and seeds the engine).
+cudaError_t launch_front_decide(unsigned* gate, unsigned* count, unsigned G, cudaStream_t s, int* launches);
 
 }  // namespace iwpp

@@ -58,7 +58,7 @@ namespace {
 bool valid_entry(const TuneEntry& e) {
     return (e.tile_rows == 32 || e.tile_rows == 64) && e.solver >= 0 && e.solver <= 2 && e.init_passes >= 0 &&
            e.init_passes <= 64 && e.queue_mult >= 0 && e.queue_mult <= 1024 && e.front_passes >= 0 &&
-           e.front_passes <= 1;
+           e.front_passes <= 2;
 }
 }  // namespace
 
@@ -137,7 +137,7 @@ int iwpp_tune_lookup(int variant, int dtype, int connectivity, long long pixels,
     out->solver = e.solver;
     out->init_passes = e.init_passes;
     out->queue_capacity = -e.queue_mult;  // negative: a multiple of the job's tile count
-    out->front_passes = e.front_passes ? 1 : 2;
+    out->front_passes = tune_front_code(e.front_passes);
     return IWPP_OK;
 }
 

@@ -56,7 +56,8 @@ class Stats(ctypes.Structure):
                 ("pushes", ctypes.c_longlong), ("rounds", ctypes.c_int), ("restarts", ctypes.c_int),
                 ("status", ctypes.c_int), ("variant", ctypes.c_int), ("device_ms", ctypes.c_double),
                 ("row_steps", ctypes.c_longlong), ("phase_cycles", ctypes.c_longlong * 5),
-                ("launches", ctypes.c_longlong), ("top_pixels", ctypes.c_longlong)]
+                ("launches", ctypes.c_longlong), ("top_pixels", ctypes.c_longlong),
+                ("front_stage", ctypes.c_longlong)]
 
     PHASES = ("queue_read", "fetch", "processing", "dump", "queue_write")
 

@@ -5,6 +5,8 @@ still violating a constraint.  Every
 result must equal the CPU oracle bit for bit, for every pixel type,
 connectivity and queue variant, on ragged and degenerate shapes, unclipped
 markers, padded pitches, batches and graph plans."""
+import os
+
 import numpy as np
 import pytest
 
@@ -31,7 +33,7 @@ def from_dev(t, dtype):
 
 def run(marker, mask, conn, variant="async", **cfg):
     m, k = to_dev(marker), to_dev(mask)
-    st = iwpp.reconstruct(m, k, connectivity=conn, variant=variant, config=iwpp.Config.make(**FRONT, **cfg))
+    st = iwpp.reconstruct(m, k, connectivity=conn, variant=variant, config=iwpp.Config.make(**{**FRONT, **cfg}))
     return from_dev(m, marker.dtype), st
 
 
@@ -41,6 +43,7 @@ def run(marker, mask, conn, variant="async", **cfg):
 def test_front_random_shapes(dt, conn, variant):
     rng = np.random.default_rng(500 + 10 * dt + conn + len(variant))
     shapes = [(1, 1), (1, 131), (131, 1), (3, 5), (64, 128), (65, 129), (200, 333), (513, 257), (130, 1029)]
+    decided_off = 0
     for i, (h, w) in enumerate(shapes):
         mask = synth.noise_mask(w, h, dt, 80 + i, 2.0, 3)
         marker = synth.sparse_marker(mask, 9 + i, 0.01) if i % 3 == 0 else \
@@ -51,7 +54,17 @@ def test_front_random_shapes(dt, conn, variant):
         assert np.array_equal(out, ref), (h, w, int((out != ref).sum()))
         # the top-level stage (6 kernels), four whole-image passes, the seed
         # check and the engine ran
-        assert st.launches >= 6 + 16 + 3
+        assert st.launches >= 6 + 16 + 3 and st.front_stage == 1
+        # decided on the device: on images this small an initial front is
+        # large against the tile count (or empty), so the stage is left out
+        # and the engine starts from the first seed check's list
+        out, st = run(marker, mask, conn, variant, front_passes=3)
+        assert st.status == 0
+        assert np.array_equal(out, ref), (h, w, "decided", int((out != ref).sum()))
+        if st.front_stage == 0:
+            assert st.top_pixels == 0
+            decided_off += 1
+    assert decided_off == len(shapes)
 
 
 @pytest.mark.parametrize("variant", VARIANTS)
@@ -102,6 +115,39 @@ def test_front_top_level_plateaus_and_corridors(dt, conn):
         assert st.status == 0
         assert np.array_equal(out, ref), (variant, int((out != ref).sum()))
         assert st.top_pixels == int((mask == top).sum())
+
+
+@pytest.mark.parametrize("variant", ["unique", "async"])
+def test_front_decided_on_the_device_takes_the_stage_for_sparse_seeds(variant):
+    # a 4096^2 spiral with four seeds: a handful of dirty tiles among 2048,
+    # so the device takes the stage
+    marker, mask, _ = synth.spiral_case(4096, 4096, 0, sigma=8.0, arm_pitch=64, nseeds=4)
+    ref = oracle.reconstruct(marker, mask, 8)
+    out, st = run(marker, mask, 8, variant, front_passes=3)
+    assert st.status == 0 and st.front_stage == 1 and st.top_pixels > 0
+    assert np.array_equal(out, ref), int((out != ref).sum())
+
+
+def test_front_untuned_default_on_large_images():
+    # 8192^2 (2^26 pixels): the untuned default decides on the device.  A
+    # spiral with few seeds takes the stage, an h-dome image does not; both
+    # results equal those of the stage forced on and forced off, and are
+    # fixed points
+    iwpp.tune_clear()
+    nt = os.cpu_count() or 1
+    spiral_m, spiral_k, _ = synth.spiral_case(8192, 8192, 0, sigma=16.0, arm_pitch=256, nseeds=16, nthreads=nt)
+    hd_k = synth.noise_mask(8192, 8192, 0, 5, 8.0, 8000, nthreads=nt)
+    hd_m = synth.hdome_marker(hd_k, 40)
+    for (marker, mask), want in (((spiral_m, spiral_k), 1), ((hd_m, hd_k), 0)):
+        m, k = to_dev(marker), to_dev(mask)
+        st = iwpp.reconstruct(m, k, connectivity=8)
+        assert st.status == 0 and st.front_stage == want
+        assert iwpp.fixed_point_violations(m, k, 8) == 0
+        got = m.cpu().numpy()
+        for fp in (1, 2):
+            out, st2 = run(marker, mask, 8, front_passes=fp)
+            assert st2.front_stage == (1 if fp == 1 else 0)
+            assert np.array_equal(out, got), (want, fp)
 
 
 @pytest.mark.parametrize("tile_rows", [32, 64])

@@ -28,9 +28,12 @@ def test_table_round_trip(tmp_path):
     p = tmp_path / "t.txt"
     # variant dtype conn pxclass batch tile_rows solver init_passes queue_mult [front_passes]
     # (a v1 line without the last field, a v2 line with it)
-    _write(p, ["3 0 8 24 0 32 1 0 0", "0 1 4 20 1 64 2 1 16 1"])
+    # (the last field: 0 no front stage, 1 always, 2 decided on the device)
+    _write(p, ["3 0 8 24 0 32 1 0 0", "0 1 4 20 1 64 2 1 16 1", "2 0 8 28 0 64 0 4 0 2"])
     iwpp.tune_load(str(p))
-    assert iwpp.tune_entries() == 2
+    assert iwpp.tune_entries() == 3
+    assert iwpp.tune_lookup("unique", 0, 8, 16384 * 16384) == {"tile_rows": 64, "solver": 0, "init_passes": 4,
+                                                                 "front_passes": 3, "queue_capacity": 0}
     # 4096 x 4096 = 2^24 pixels: class 24
     assert iwpp.tune_lookup("async", 0, 8, 4096 * 4096) == {"tile_rows": 32, "solver": 1, "init_passes": 0,
                                                           "front_passes": 2, "queue_capacity": 0}
@@ -42,7 +45,8 @@ def test_table_round_trip(tmp_path):
     iwpp.tune_save(str(q))
     lines = [ln.split() for ln in open(q) if not ln.startswith("#")]
     assert sorted(lines) == sorted([["0", "1", "4", "20", "1", "64", "2", "1", "16", "1"],
-                                    ["3", "0", "8", "24", "0", "32", "1", "0", "0", "0"]])
+                                    ["3", "0", "8", "24", "0", "32", "1", "0", "0", "0"],
+                                    ["2", "0", "8", "28", "0", "64", "0", "4", "0", "2"]])
     iwpp.tune_clear()
     assert iwpp.tune_entries() == 0
 
@@ -52,7 +56,7 @@ def test_malformed_table_changes_nothing(tmp_path):
     good = tmp_path / "good.txt"
     _write(good, ["3 0 8 24 0 64 0 0 0"])
     iwpp.tune_load(str(good))
-    for bad_line in ["3 0 8 24 0 48 0 0 0", "3 0 8 24 0 64 7 0 0", "3 0 8", "x y z", "3 0 8 24 0 64 0 0 0 5",
+    for bad_line in ["3 0 8 24 0 48 0 0 0", "3 0 8 24 0 64 7 0 0", "3 0 8", "x y z", "3 0 8 24 0 64 0 0 0 3",
                      "3 0 8 24 0 64 0 0 0 1 9"]:
         bad = tmp_path / "bad.txt"
         _write(bad, ["3 1 8 20 0 32 1 0 0", bad_line])
