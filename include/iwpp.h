@@ -34,9 +34,12 @@ typedef enum iwpp_status {
     IWPP_ERR_NO_DEVICE = 6, /* no CUDA device, or not a GB300-class (sm_103) one */
     IWPP_ERR_BUSY = 7,      /* a server's queue is full or it is shutting down; a
                                waited-for request is not finished yet */
-    IWPP_ERR_TOO_LARGE = 8  /* the image needs more workspace than the static scratch of
+    IWPP_ERR_TOO_LARGE = 8, /* the image needs more workspace than the static scratch of
                                iwpp_reconstruct_noalloc holds, or more device memory
                                than a server's budget */
+    IWPP_ERR_INTERNAL = 9   /* a device-side consistency check failed (a queue entry that
+                               names no tile): a library defect, reported instead of
+                               touching memory outside the job */
 } iwpp_status;
 
 typedef enum iwpp_dtype { IWPP_U8 = 0, IWPP_U16 = 1, IWPP_I32 = 2 } iwpp_dtype;
@@ -292,7 +295,7 @@ typedef struct iwpp_server_config {
     int max_batch;             /* requests per batch, 0 = 256 */
     int max_pending;           /* waiting requests before submit says BUSY, 0 = 65536 */
     int variant;               /* queue variant, IWPP_QUEUE_DEFAULT = async */
-    int tile_rows;             /* 0 = default */
+    int tile_rows;             /* 0 = default; batches run the tile engine alone (front_passes 2) */
     int lane_ctas;             /* CTAs per batch launch, 0 = the whole GPU */
     int timeout_ms;            /* device wait bound per batch, 0 = 60000 */
     long long memory_budget;   /* device bytes for admitted requests, 0 = half the free memory at creation */

@@ -731,6 +731,7 @@ int read_stats(Ctrl* host_ctrl, const Workspace& ws, cudaStream_t s, long long t
     int st = IWPP_OK;
     if (host_ctrl->error == DEV_ERR_TIMEOUT) st = IWPP_ERR_TIMEOUT;
     if (host_ctrl->error == DEV_ERR_OVERFLOW) st = IWPP_ERR_OVERFLOW;
+    if (host_ctrl->error == DEV_ERR_INTERNAL) st = IWPP_ERR_INTERNAL;
     if (out) {
         out->tiles = tiles;
         out->visits = (long long)host_ctrl->visits;
@@ -852,6 +853,7 @@ const char* iwpp_status_string(int status) {
         case IWPP_ERR_NO_DEVICE: return "no sm_103 (GB300) CUDA device";
         case IWPP_ERR_BUSY: return "server queue full, shutting down, or request not finished";
         case IWPP_ERR_TOO_LARGE: return "image too large for the no-allocation scratch or the server budget";
+        case IWPP_ERR_INTERNAL: return "a device-side consistency check failed";
         default: return "unknown status";
     }
 }
@@ -974,6 +976,7 @@ int iwpp_handle_sync(iwpp_handle h, iwpp_stats* stats) {
     int st = IWPP_OK;
     if (c.error == DEV_ERR_TIMEOUT) st = IWPP_ERR_TIMEOUT;
     if (c.error == DEV_ERR_OVERFLOW) st = IWPP_ERR_OVERFLOW;
+    if (c.error == DEV_ERR_INTERNAL) st = IWPP_ERR_INTERNAL;
     if (stats) {
         stats->tiles = h->last_tiles;
         stats->visits = (long long)c.visits;
@@ -1093,6 +1096,7 @@ int iwpp_plan_sync(iwpp_plan p, iwpp_stats* stats) {
     int st = IWPP_OK;
     if (c.error == DEV_ERR_TIMEOUT) st = IWPP_ERR_TIMEOUT;
     if (c.error == DEV_ERR_OVERFLOW) st = IWPP_ERR_OVERFLOW;
+    if (c.error == DEV_ERR_INTERNAL) st = IWPP_ERR_INTERNAL;
     if (stats) {
         stats->tiles = p->tiles;
         stats->visits = (long long)c.visits;

@@ -93,6 +93,42 @@ __device__ __forceinline__ void mutex_unlock(const EngineArgs& a, unsigned ticke
 // (IWPP MP DQ/src/globalQueue.cu:14-47).  A short insertion sets the
 // overflow flag (the reference's memLeak, MR.cu:524-526); the tiles stay
 // DIRTY and are recovered by the restart.
+// The mutex stack's insertion: one lock acquisition for the warp's entries.
+// `counted`: `pending` already holds them (entries moving from a CTA
+// buffer); else they are added to it before the release can publish them.
+__device__ void mutex_push_global(const EngineArgs& a, bool want, unsigned gn, int lane, bool counted) {
+    const unsigned ballot = __ballot_sync(FULL, want);
+    if (ballot == 0u) return;
+    const int n = __popc(ballot);
+    const int rank = __popc(ballot & ((1u << lane) - 1u));
+    int base = -1;
+    unsigned ticket = 0u;
+    if (lane == 0) {
+        if (mutex_lock(a, &ticket)) {
+            const int top = ld_volatile(&a.ctrl->top);
+            if ((unsigned)top + (unsigned)n <= a.cap) {
+                base = top;
+                if (!counted) atomicAdd(&a.ctrl->pending, n);  // before the entries can be taken
+            } else {
+                atomicExch(&a.ctrl->overflow, 1u);
+                if (counted) atomicSub(&a.ctrl->pending, n);  // lost: the restart recovers the tiles
+                mutex_unlock(a, ticket);
+            }
+        }
+    }
+    base = __shfl_sync(FULL, base, 0);
+    if (base < 0) return;
+    if (want) {
+        a.q0[base + rank] = gn;
+        __threadfence();  // the entry before the release that publishes it
+    }
+    __syncwarp();
+    if (lane == 0) {
+        *(volatile int*)&a.ctrl->top = base + n;
+        mutex_unlock(a, ticket);
+    }
+}
+
 template <int VAR>
 __device__ void push_entries(const EngineArgs& a, bool want, unsigned gn, int lane, unsigned* wq,
                              WarpCounters& cnt) {
@@ -101,31 +137,7 @@ __device__ void push_entries(const EngineArgs& a, bool want, unsigned gn, int la
     const int n = __popc(ballot);
     const int rank = __popc(ballot & ((1u << lane) - 1u));
     if (VAR == VAR_MUTEX) {
-        int base = -1;
-        unsigned ticket = 0u;
-        if (lane == 0) {
-            if (mutex_lock(a, &ticket)) {
-                const int top = ld_volatile(&a.ctrl->top);
-                if ((unsigned)top + (unsigned)n <= a.cap) {
-                    base = top;
-                    atomicAdd(&a.ctrl->pending, n);  // before the entries can be taken
-                } else {
-                    atomicExch(&a.ctrl->overflow, 1u);
-                    mutex_unlock(a, ticket);
-                }
-            }
-        }
-        base = __shfl_sync(FULL, base, 0);
-        if (base < 0) return;
-        if (want) {
-            a.q0[base + rank] = gn;
-            __threadfence();  // the entry before the release that publishes it
-        }
-        __syncwarp();
-        if (lane == 0) {
-            *(volatile int*)&a.ctrl->top = base + n;
-            mutex_unlock(a, ticket);
-        }
+        mutex_push_global(a, want, gn, lane, false);
     } else if (VAR == VAR_ASYNC) {
         // positions [base, base + n) of the ring; `pending` first, so the job
         // cannot look finished while these entries exist
@@ -163,6 +175,105 @@ __device__ void push_entries(const EngineArgs& a, bool want, unsigned gn, int la
     cnt.pushes += (unsigned)n;
 }
 
+// ------------------------------------------------- mutex: CTA buffers
+// The MP discipline keeps one LIFO stack under one lock, and what
+// serialises it is one acquisition per insertion and per take.  Each CTA
+// therefore keeps the entries its warps insert in a shared-memory buffer and
+// takes from it first; the global stack sees a batch take when the buffer
+// runs dry, a spill when it fills, and a share when the global stack is empty
+// while warps elsewhere wait.  Buffered entries count in `pending`, so the
+// termination rule (nothing pending, nothing stacked) is unchanged.
+constexpr int kCtaBuf = 64;    // entries a CTA buffers
+constexpr int kCtaSpill = 48;  // above this a push spills the buffer down to kCtaKeep
+constexpr int kCtaKeep = 16;
+
+struct MutexCtaBuf {
+    int lock;
+    int n;
+    unsigned e[kCtaBuf];
+};
+__shared__ MutexCtaBuf s_cq;
+
+// The buffer's lock, held by one of this CTA's warps for a few shared-memory
+// accesses at a time; the bound is never reached in a working job.
+__device__ __forceinline__ bool cq_lock(const EngineArgs& a) {
+    unsigned spins = 0;
+    while (atomicCAS(&s_cq.lock, 0, 1) != 0) {
+        __nanosleep(32);
+        if (++spins > (1u << 22)) {
+            set_error(a.ctrl, DEV_ERR_TIMEOUT);
+            return false;
+        }
+    }
+    __threadfence_block();
+    return true;
+}
+__device__ __forceinline__ void cq_unlock() {
+    __threadfence_block();
+    atomicExch(&s_cq.lock, 0);
+}
+
+__device__ __forceinline__ int cq_count() { return *(volatile int*)&s_cq.n; }
+
+// Moves up to 32 of the buffer's newest entries beyond `keep` to the global
+// stack (one acquisition).
+__device__ void cta_spill(const EngineArgs& a, int lane, int keep) {
+    int m = 0, base = 0;
+    if (lane == 0 && cq_lock(a)) {
+        m = min(max(s_cq.n - keep, 0), 32);
+        s_cq.n -= m;
+        base = s_cq.n;
+        if (m == 0) cq_unlock();
+    }
+    m = __shfl_sync(FULL, m, 0);
+    base = __shfl_sync(FULL, base, 0);
+    if (m == 0) return;
+    const unsigned mine = lane < m ? *(volatile unsigned*)&s_cq.e[base + lane] : 0u;
+    __syncwarp();
+    if (lane == 0) cq_unlock();
+    mutex_push_global(a, lane < m, mine, lane, true);
+}
+
+// Inserts the entries of the lanes with `want` set into this CTA's buffer
+// (what does not fit goes to the global stack), spilling a full buffer.
+// `counted`: `pending` already holds them.
+__device__ void cta_push(const EngineArgs& a, bool want, unsigned gn, int lane, WarpCounters& cnt,
+                         bool counted = false) {
+    const unsigned ballot = __ballot_sync(FULL, want);
+    if (ballot == 0u) return;
+    const int n = __popc(ballot);
+    const int rank = __popc(ballot & ((1u << lane) - 1u));
+    int base = 0, k = 0;
+    bool locked = false;
+    if (lane == 0) {
+        if (!counted) atomicAdd(&a.ctrl->pending, n);  // before any of them can be taken
+        locked = cq_lock(a);
+        if (locked) {
+            k = min(n, kCtaBuf - s_cq.n);
+            base = s_cq.n;
+            s_cq.n += k;
+        }
+    }
+    k = __shfl_sync(FULL, k, 0);
+    base = __shfl_sync(FULL, base, 0);
+    if (want && rank < k) *(volatile unsigned*)&s_cq.e[base + rank] = gn;
+    __syncwarp();
+    if (locked) cq_unlock();
+    if (!counted) cnt.pushes += (unsigned)n;
+    if (n > k) mutex_push_global(a, want && rank >= k, gn, lane, true);
+    if (__shfl_sync(FULL, cq_count(), 0) > kCtaSpill) cta_spill(a, lane, kCtaKeep);
+}
+
+// The buffer's newest entry, or ~0u.
+__device__ unsigned cta_take(const EngineArgs& a, int lane) {
+    unsigned g = ~0u;
+    if (lane == 0 && cq_count() > 0 && cq_lock(a)) {
+        if (s_cq.n > 0) g = *(volatile unsigned*)&s_cq.e[--s_cq.n];
+        cq_unlock();
+    }
+    return __shfl_sync(FULL, g, 0);
+}
+
 // Marks the neighbour tiles in `nb` DIRTY and inserts them (VAR_UNIQUE /
 // VAR_ASYNC: only those that were neither pending nor being visited).  With
 // the async queue one of the newly dirty tiles is not inserted but returned:
@@ -194,7 +305,10 @@ __device__ unsigned notify(const EngineArgs& a, const ImgDesc& d, int tx, int ty
             if (lane == leader) want = false;
         }
     }
-    push_entries<VAR>(a, want, gn, lane, wq, cnt);
+    if (VAR == VAR_MUTEX)
+        cta_push(a, want, gn, lane, cnt);
+    else
+        push_entries<VAR>(a, want, gn, lane, wq, cnt);
     return cont;
 }
 
@@ -296,139 +410,172 @@ __device__ bool process_entry(const EngineArgs& a, unsigned g, WarpSmem<TH>& sm,
     const long long q1 = clock64();
     if (lane == 0) old = atomicAnd(&a.state[g], ~ST_ACTIVE);
     old = __shfl_sync(FULL, old, 0);
-    if (old & ST_DIRTY) push_entries<VAR>(a, lane == 0, g, lane, wq, cnt);
+    if (old & ST_DIRTY) {
+        if (VAR == VAR_MUTEX)
+            cta_push(a, lane == 0, g, lane, cnt);
+        else
+            push_entries<VAR>(a, lane == 0, g, lane, wq, cnt);
+    }
     cnt.phase[4] += clock64() - q1;
     return true;
 }
 
 // ------------------------------------------------------- mutex worker
-// One persistent launch; warps take up to kMutexBatch entries per lock
-// acquisition from the LIFO stack (the reference takes one,
-// IWPP MP/src/MorphologicalReconstruction.cu:221).  Termination: the stack
-// is empty and no taken entry is unfinished (`pending` == 0), which replaces
-// activeBlocksCount (IWPP MP/src/globalQueue.cu:134-145).  On overflow the
-// quiescent stack is refilled with every tile (MR.cu:785-806).
+// One persistent launch.  A warp takes its next entry from its CTA's buffer;
+// when that is empty, it takes a share of the global LIFO stack under the
+// lock (up to kMutexBatch entries, the stack divided among the CTAs; the
+// reference takes one, IWPP MP/src/MorphologicalReconstruction.cu:221),
+// keeps the first and buffers the rest for its CTA.  Termination: nothing
+// is stacked and no inserted entry is unfinished (`pending` == 0, buffered
+// entries included), which replaces activeBlocksCount
+// (IWPP MP/src/globalQueue.cu:134-145).  On overflow the quiescent stack is
+// refilled with every tile (MR.cu:785-806).
 template <int TH>
 __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, WarpCounters& cnt, unsigned& phase) {
+    if (threadIdx.x == 0) {
+        s_cq.lock = 0;
+        s_cq.n = 0;
+    }
+    __syncthreads();
     long long idle_since = 0;
     unsigned idle_progress = 0u;
     unsigned ns = 64;
+    bool idle = false;  // counted in ctrl->idle
+    auto leave_idle = [&]() {
+        if (idle && lane == 0) atomicSub(&a.ctrl->idle, 1u);
+        idle = false;
+    };
     for (;;) {
-        int n = 0, base = 0, verdict = 0;  // verdict: 0 work/retry, 1 exit, 2 refill
+        if (ld_volatile(&a.ctrl->error) != 0u) break;
         const long long qr0 = clock64();
-        // Look before queueing for the lock: an idle warp takes a ticket only
-        // while the stack holds more entries than there are warps in line
-        // (a ticket lock serves in arrival order, so idle warps queued for an
-        // empty stack would delay every warp that inserts), or when the job
-        // looks finished but an overflow needs the refill.  A finished job
-        // (no entry in the stack or in flight, no overflow) is left without
-        // the lock.
-        if (ld_volatile(&a.ctrl->error) != 0u) return;
-        int look = 0;  // 0 back off, 1 take a ticket, 2 finished
-        if (lane == 0) {
-            const int top = ld_volatile(&a.ctrl->top);
-            const int pend = ld_volatile(&a.ctrl->pending);
-            const unsigned line = ld_volatile(&a.ctrl->lock_next) - ld_volatile(&a.ctrl->lock_serving);
-            if (pend == 0 && top == 0 && ld_volatile(&a.ctrl->overflow) == 0u)
-                look = 2;
-            else if (top > (int)line || pend == 0)
-                look = 1;
-        }
-        look = __shfl_sync(FULL, look, 0);
-        if (look == 2) return;
-        const bool try_lock = look == 1;
-        unsigned ticket = 0u;
-        if (lane == 0 && try_lock) {
-            if (!mutex_lock(a, &ticket)) {
-                verdict = 1;
-            } else {
+        unsigned g = cta_take(a, lane);
+        if (g == ~0u) {
+            int n = 0, base = 0, verdict = 0;  // verdict: 0 work/retry, 1 exit, 2 refill
+            // Look before queueing for the lock: an idle warp takes a ticket
+            // only while the stack holds more entries than there are warps in
+            // line (a ticket lock serves in arrival order, so idle warps
+            // queued for an empty stack would delay every warp that
+            // inserts), or when the job looks finished but an overflow needs
+            // the refill.  A finished job (no entry in the stack or pending,
+            // no overflow) is left without the lock.
+            int look = 0;  // 0 back off, 1 take a ticket, 2 finished
+            if (lane == 0) {
                 const int top = ld_volatile(&a.ctrl->top);
-                if (top > 0) {
-                    // a share that leaves entries for other warps while the
-                    // stack is short, up to kMutexBatch while it is long
-                    n = top >> 8;
-                    n = n < 1 ? 1 : n > kMutexBatch ? kMutexBatch : n;
-                    base = top - n;
-                } else if (ld_volatile(&a.ctrl->pending) == 0) {
-                    if (ld_volatile(&a.ctrl->overflow) != 0u) {
-                        if ((int)ld_volatile(&a.ctrl->restarts) >= a.max_restarts) {
-                            set_error(a.ctrl, DEV_ERR_OVERFLOW);
-                            verdict = 1;
-                        } else {
-                            verdict = 2;
-                        }
-                    } else {
-                        verdict = 1;
-                    }
-                }
-                if (n == 0 && verdict != 2) mutex_unlock(a, ticket);
+                const int pend = ld_volatile(&a.ctrl->pending);
+                const unsigned line = ld_volatile(&a.ctrl->lock_next) - ld_volatile(&a.ctrl->lock_serving);
+                if (pend == 0 && top == 0 && ld_volatile(&a.ctrl->overflow) == 0u)
+                    look = 2;
+                else if (top > (int)line || pend == 0)
+                    look = 1;
             }
-        }
-        n = __shfl_sync(FULL, n, 0);
-        base = __shfl_sync(FULL, base, 0);
-        verdict = __shfl_sync(FULL, verdict, 0);
-        if (verdict == 1) return;
-        if (verdict == 2) {
-            // quiescent with lost insertions: refill with every tile (lock held)
-            for (unsigned i = (unsigned)lane; i < a.G && i < a.cap; i += 32u) a.q0[i] = a.G - 1u - i;
+            look = __shfl_sync(FULL, look, 0);
+            if (look == 2) break;
+            unsigned ticket = 0u;
+            if (lane == 0 && look == 1) {
+                if (!mutex_lock(a, &ticket)) {
+                    verdict = 1;
+                } else {
+                    const int top = ld_volatile(&a.ctrl->top);
+                    if (top > 0) {
+                        // the stack divided among the CTAs, at most a batch
+                        n = top / (int)gridDim.x;
+                        n = n < 1 ? 1 : n > kMutexBatch ? kMutexBatch : n;
+                        base = top - n;
+                    } else if (ld_volatile(&a.ctrl->pending) == 0) {
+                        if (ld_volatile(&a.ctrl->overflow) != 0u) {
+                            if ((int)ld_volatile(&a.ctrl->restarts) >= a.max_restarts) {
+                                set_error(a.ctrl, DEV_ERR_OVERFLOW);
+                                verdict = 1;
+                            } else {
+                                verdict = 2;
+                            }
+                        } else {
+                            verdict = 1;
+                        }
+                    }
+                    if (n == 0 && verdict != 2) mutex_unlock(a, ticket);
+                }
+            }
+            n = __shfl_sync(FULL, n, 0);
+            base = __shfl_sync(FULL, base, 0);
+            verdict = __shfl_sync(FULL, verdict, 0);
+            if (verdict == 1) break;
+            if (verdict == 2) {
+                // quiescent with lost insertions: refill with every tile (lock held)
+                for (unsigned i = (unsigned)lane; i < a.G && i < a.cap; i += 32u) a.q0[i] = a.G - 1u - i;
+                __syncwarp();
+                if (lane == 0) {
+                    const int cnt_all = (int)(a.G < a.cap ? a.G : a.cap);
+                    atomicAdd(&a.ctrl->pending, cnt_all);
+                    atomicExch(&a.ctrl->overflow, 0u);
+                    atomicAdd(&a.ctrl->restarts, 1u);
+                    __threadfence();
+                    *(volatile int*)&a.ctrl->top = cnt_all;
+                    mutex_unlock(a, ticket);
+                }
+                __syncwarp();
+                continue;
+            }
+            if (n == 0) {
+                // nothing to take but work in flight: back off, bounded by progress
+                if (!idle) {
+                    if (lane == 0) atomicAdd(&a.ctrl->idle, 1u);
+                    idle = true;
+                }
+                const unsigned prog = ld_volatile(&a.ctrl->progress);
+                const long long now = globaltimer_ns();
+                if (idle_since == 0 || prog != idle_progress) {
+                    idle_since = now;
+                    idle_progress = prog;
+                } else if (now - idle_since > a.timeout_ns) {
+                    if (lane == 0) set_error(a.ctrl, DEV_ERR_TIMEOUT);
+                    break;
+                }
+                __nanosleep(ns);
+                if (ns < 2048) ns <<= 1;
+                cnt.phase[0] += clock64() - qr0;
+                continue;
+            }
+            // copy the taken entries out before the lock is released: the
+            // first is this warp's, the rest go to the CTA's buffer
+            unsigned mine = 0u;
+            if (lane < n) mine = __ldcg(&a.q0[base + lane]);  // from L2: the slot may have been cached before
             __syncwarp();
             if (lane == 0) {
-                const int cnt_all = (int)(a.G < a.cap ? a.G : a.cap);
-                atomicAdd(&a.ctrl->pending, cnt_all);
-                atomicExch(&a.ctrl->overflow, 0u);
-                atomicAdd(&a.ctrl->restarts, 1u);
-                __threadfence();
-                *(volatile int*)&a.ctrl->top = cnt_all;
+                *(volatile int*)&a.ctrl->top = base;
                 mutex_unlock(a, ticket);
             }
-            __syncwarp();
-            continue;
+            g = __shfl_sync(FULL, mine, 0);
+            cta_push(a, lane >= 1 && lane < n, mine, lane, cnt, true);
         }
-        if (n == 0) {
-            // nothing to take but work in flight: back off, bounded by progress
-            const unsigned prog = ld_volatile(&a.ctrl->progress);
-            const long long now = globaltimer_ns();
-            if (idle_since == 0 || prog != idle_progress) {
-                idle_since = now;
-                idle_progress = prog;
-            } else if (now - idle_since > a.timeout_ns) {
-                if (lane == 0) set_error(a.ctrl, DEV_ERR_TIMEOUT);
-                return;
-            }
-            if (ld_volatile(&a.ctrl->error) != 0u) return;
-            __nanosleep(ns);
-            if (ns < 2048) ns <<= 1;
-            cnt.phase[0] += clock64() - qr0;
-            continue;
-        }
+        leave_idle();
         idle_since = 0;
         ns = 64;
         cnt.phase[0] += clock64() - qr0;
-        // copy the taken entries out before the lock is released
-        unsigned mine = 0u;
-        if (lane < n) mine = a.q0[base + lane];
-        __syncwarp();
+        if (g >= a.G) {  // a consistency check: an entry names no tile
+            if (lane == 0) set_error(a.ctrl, DEV_ERR_INTERNAL);
+            break;
+        }
+        bool ok = true;
+        for (;;) {  // the entry, then the newly dirty neighbours it leaves behind
+            unsigned nxt = ~0u;
+            ok = process_entry<VAR_MUTEX, TH>(a, g, sm, lane, nullptr, cnt, phase, &nxt);
+            if (!ok || nxt == ~0u) break;
+            g = nxt;
+        }
+        if (!ok) break;
         if (lane == 0) {
-            *(volatile int*)&a.ctrl->top = base;
-            mutex_unlock(a, ticket);
+            __threadfence();
+            atomicAdd(&a.ctrl->progress, 1u);
+            atomicSub(&a.ctrl->pending, 1);  // after this entry's insertions
         }
-        for (int j = 0; j < n; ++j) {
-            unsigned g = __shfl_sync(FULL, mine, j);
-            bool ok = true;
-            for (;;) {  // the entry, then the newly dirty neighbours it leaves behind
-                unsigned nxt = ~0u;
-                ok = process_entry<VAR_MUTEX, TH>(a, g, sm, lane, nullptr, cnt, phase, &nxt);
-                if (!ok || nxt == ~0u) break;
-                g = nxt;
-            }
-            if (!ok) return;
-            if (lane == 0) {
-                __threadfence();
-                atomicAdd(&a.ctrl->progress, 1u);
-                atomicSub(&a.ctrl->pending, 1);  // after this entry's insertions
-            }
-        }
+        // share: the global stack is empty while warps elsewhere wait
+        int share = 0;
+        if (lane == 0 && cq_count() >= 2 && ld_volatile(&a.ctrl->top) == 0 && ld_volatile(&a.ctrl->idle) > 0u)
+            share = 1;
+        if (__shfl_sync(FULL, share, 0)) cta_spill(a, lane, __shfl_sync(FULL, cq_count(), 0) / 2);
     }
+    leave_idle();
 }
 
 // ------------------------------------------------------- async worker
@@ -674,6 +821,7 @@ __global__ void engine_init_kernel(EngineArgs a, int variant) {
         c->top = (int)(n0 < a.cap ? n0 : a.cap);
         c->pending = (int)(n0 < a.cap ? n0 : a.cap);
         c->progress = 0u;
+        c->idle = 0u;
         c->ahead = 0u;
         c->atail = n0;
         c->ninit = n0;

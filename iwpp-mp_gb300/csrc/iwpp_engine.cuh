@@ -35,7 +35,7 @@ namespace iwpp {
 // halo pixels rose since the tile last converged.
 enum : unsigned { ST_DIRTY = 1u, ST_ACTIVE = 2u, ST_SIDE_SHIFT = 8u, ST_SIDES = 0xffu << 8 };
 enum : int { VAR_MUTEX = 0, VAR_DOUBLE = 1, VAR_UNIQUE = 2, VAR_ASYNC = 3 };
-enum : unsigned { DEV_OK = 0u, DEV_ERR_TIMEOUT = 3u, DEV_ERR_OVERFLOW = 5u };
+enum : unsigned { DEV_OK = 0u, DEV_ERR_TIMEOUT = 3u, DEV_ERR_OVERFLOW = 5u, DEV_ERR_INTERNAL = 9u };
 
 constexpr int kWarps = 4;       // warps (independent tile workers) per CTA
 constexpr int kMutexBatch = 8;  // entries taken per mutex acquisition
@@ -68,6 +68,7 @@ struct Ctrl {
     unsigned long long top_pixels;    // pixels the top-level stage labelled
     unsigned ninit;     // initial entries (every tile, or the seed list after front passes)
     unsigned front_gate;  // front stage decided on the device: 1 run it, 0 leave the job to the engine
+    unsigned idle;        // mutex: warps waiting for work
 };
 
 struct EngineArgs {

@@ -277,6 +277,11 @@ int iwpp_server_create(iwpp_server* out, int device, const iwpp_server_config* c
     s->cfg.init_passes = -1;
     s->cfg.grid_ctas = c.lane_ctas;
     s->cfg.timeout_ms = c.timeout_ms ? c.timeout_ms : 60000;
+    // Batches of independent requests go to the tile engine alone: the front
+    // stage's scratch is not in the lane workspaces sized below (a workspace
+    // that grows mid-stream synchronises the device), and the decision it
+    // makes would be one for the whole mixed batch.
+    s->cfg.front_passes = 2;
 
     int prev = 0;
     cudaGetDevice(&prev);

@@ -74,8 +74,9 @@ def test_front_spirals_and_config0(variant):
         ref = oracle.reconstruct(marker, mask, 8)
         out, st = run(marker, mask, 8, variant)
         assert np.array_equal(out, ref), (dt, int((out != ref).sum()))
-        # the corridor is carried by the passes: the engine only finishes
-        assert st.visits < st.tiles
+        # the corridor is carried by the stage: the engine only finishes
+        # (alone it revisits the tiles along the corridor many times over)
+        assert st.visits < 2 * st.tiles
     marker, mask = synth.config0()
     ref = oracle.reconstruct(marker, mask, 8)
     out, _ = run(marker, mask, 8, variant)
