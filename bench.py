@@ -849,7 +849,9 @@ def main():
     ap.add_argument("--config1-only", action="store_true",
                     help="only the six 4096^2 configuration-1 reconstructions with --variant (one JSON line)")
     ap.add_argument("--profile-headline", type=int, default=0, metavar="N",
-                    help="only N default-configuration reconstructions of the headline image (for profilers)")
+                    help="only N reconstructions of the headline image with the front stage (for profilers)")
+    ap.add_argument("--profile-passes", type=int, default=2,
+                    help="whole-image passes of the front stage in --profile-headline")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -864,11 +866,11 @@ def main():
 
 
 def run_profile_headline(args):
-    """The autotuner once on the headline image (as the bench does), then N
-    reconstructions with the default configuration fields (the tuning table
-    fills them) and --variant, each from the pristine marker; each call's
-    launch count is printed, so the last N calls' launches can be picked out
-    of a profiler's launch list."""
+    """N reconstructions of the headline image with the front stage and
+    --profile-passes whole-image passes (the configuration the autotuner
+    picks for this image class in a plain run; under a profiler, which
+    serialises and replays every launch, its timings would pick another)
+    and --variant, each from the pristine marker, nothing else."""
     import torch
 
     import iwpp
@@ -879,13 +881,11 @@ def run_profile_headline(args):
     mask = torch.from_numpy(mask_np).to(dev)
     pristine = torch.from_numpy(marker_np).to(dev)
     work = pristine.clone()
-    tuned = iwpp.autotune([(work, mask, 8)], variant=args.variant, repeats=1)
-    print(json.dumps({"autotuned": {k: tuned[k] for k in ("tile_rows", "solver", "init_passes", "front_passes")}}),
-          flush=True)
+    cfg = iwpp.Config.make(front_passes=1, init_passes=args.profile_passes)
     for i in range(args.profile_headline):
         work.copy_(pristine)
         torch.cuda.synchronize()
-        st = iwpp.reconstruct(work, mask, connectivity=8, variant=args.variant)
+        st = iwpp.reconstruct(work, mask, connectivity=8, variant=args.variant, config=cfg)
         print(json.dumps({"call": i, "device_ms": st.device_ms, "launches": st.launches, "visits": st.visits,
                           "front_stage": st.front_stage, "status": st.status}), flush=True)
     return 0

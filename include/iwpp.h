@@ -74,7 +74,8 @@ typedef struct iwpp_config {
                                   pitch are 16-byte aligned) */
     int solver;                /* in-tile solver: 0 = automatic, 1 = row sweeps (fewest
                                   instructions), 2 = vertical / horizontal passes
-                                  (shortest latency) */
+                                  (shortest latency), 3 = revisits by a per-tile pixel
+                                  queue in shared memory (first visits by passes) */
     int front_passes;          /* the front stage: the pixels at the mask's largest value
                                   raised by connected-component labelling, init_passes
                                   whole-image passes (default 4), and the tile engine started

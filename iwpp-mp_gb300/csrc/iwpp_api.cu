@@ -74,7 +74,7 @@ Config resolve_config(const iwpp_config* c) {
     r.timeout_ms = c && c->timeout_ms > 0 ? c->timeout_ms : 10000;
     r.clip_marker = c ? c->clip_marker : 0;
     r.plain_loads = c ? c->plain_loads : 0;
-    r.solver = c && c->solver >= 0 && c->solver <= 2 ? c->solver : 0;
+    r.solver = c && c->solver >= 0 && c->solver <= 3 ? c->solver : 0;
     r.front_passes = c && c->front_passes >= 0 && c->front_passes <= 3 ? c->front_passes : 0;
     r.phantom_work = c && c->phantom_work == 1 ? 1 : 0;
     r.dflt_tile = r.tile_rows == 0;
@@ -1292,12 +1292,12 @@ int iwpp_autotune(iwpp_handle h, const iwpp_image* images, int n, int variant, i
                 c.front_passes = 2;
                 consider(c, !front_default && th == dflt_th && solver == 0);
             }
-        // stage 2: the front stage (top-level labelling, then 2 / 4 / 8
+        // stage 2: the front stage (top-level labelling, then 1 / 2 / 3 / 4 / 8
         // whole-image passes, then the engine from the seed check) with the
         // best tile height and solver; long propagation paths want it
         if (best_ms >= 0.0) {
             const iwpp_config base = best;
-            for (int ip : {2, 4, 8}) {
+            for (int ip : {1, 2, 3, 4, 8}) {
                 iwpp_config c = base;
                 c.front_passes = 1;
                 c.init_passes = ip;

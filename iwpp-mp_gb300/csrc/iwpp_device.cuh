@@ -147,6 +147,7 @@ __device__ __constant__ static const int kNbDy[8] = {-1, 1, 0, 0, -1, -1, 1, 1};
 // SMEM row r holds image row y0 - 1 + r: row 0 is the halo above the tile,
 // rows 1..TH the tile, row TH+1 the halo below.  hL* / hR* hold the left /
 // right halo column pixels of the same rows.
+constexpr int kPqCap = 448;  // pixel-queue solver: FIFO entries per warp
 template <int TH>
 struct __align__(128) WarpSmem {
     uint32_t tm[(TH + 2) * 32];
@@ -156,6 +157,7 @@ struct __align__(128) WarpSmem {
     uint32_t hRm[TH + 2];
     uint32_t hRk[TH + 2];
     unsigned long long mbar;
+    unsigned short pq[kPqCap];  // pixel-queue solver: tile pixel indices r * TW + c
 };
 
 // ------------------------------------------------------- async-copy helpers
@@ -429,18 +431,29 @@ __device__ __forceinline__ unsigned long long vpass(WarpSmem<TH>& sm, int lane, 
     unsigned long long chg = 0ull;
     uint32_t diff = 0u;
     if (CONN == 4) {
-        // columns are independent: one packed min / max per word and row
-        uint32_t prevw = sm.tm[(DOWN ? first - 1 : first + 1) * 32 + lane];
+        // columns are independent: packed min / max per word and row; uint8
+        // words run as two u16x2 chains (even and odd bytes), whose min / max
+        // are single instructions, so the chain is two of them per row
+        const uint32_t first_prev = sm.tm[(DOWN ? first - 1 : first + 1) * 32 + lane];
+        uint32_t plo = first_prev & 0x00ff00ffu, phi = (first_prev >> 8) & 0x00ff00ffu, prevw = first_prev;
 #pragma unroll 4
         for (int i = 0; i < count; ++i) {
             const int r = DOWN ? first + i : first - i;
             const uint32_t old = sm.tm[r * 32 + lane];
-            const uint32_t nw = word_max<DT>(old, word_min<DT>(prevw, sm.tk[r * 32 + lane]));
+            const uint32_t kw = sm.tk[r * 32 + lane];
+            uint32_t nw;
+            if (DT == DT_U8) {
+                plo = __vmaxu2(old & 0x00ff00ffu, __vminu2(plo, kw & 0x00ff00ffu));
+                phi = __vmaxu2((old >> 8) & 0x00ff00ffu, __vminu2(phi, (kw >> 8) & 0x00ff00ffu));
+                nw = plo | (phi << 8);
+            } else {
+                nw = word_max<DT>(old, word_min<DT>(prevw, kw));
+                prevw = nw;
+            }
             sm.tm[r * 32 + lane] = nw;
             const uint32_t x = nw ^ old;
             diff |= x;
             if (x != 0u) chg |= 1ull << (r - 1);
-            prevw = nw;
         }
         col_now |= (diff & edge_mask) != 0u;
         __syncwarp();
@@ -726,10 +739,150 @@ __device__ __forceinline__ unsigned detect_neighbours(const WarpSmem<TH>& sm, in
 struct NoEarlyFlush {
     static constexpr bool kEnabled = false;
     bool use_passes;
+    bool use_pq;  // revisits by the pixel queue (pq_solve)
     __device__ bool passes(int) { return use_passes; }
+    __device__ bool pq() { return use_pq; }
     __device__ bool want(int) { return false; }
     __device__ void flush(unsigned, int) {}
 };
+
+// ------------------------------------------------------- pixel queue
+// Third in-tile solver, for revisits: a FIFO of tile pixels in shared memory
+// instead of whole-tile passes.  Seeds: the pixels of the tile's boundary
+// ring whose constraint towards any neighbour (halo included) is violated;
+// each is raised to what its neighbours allow and queued.  A round pops up to
+// 32 pixels, one per lane; each raises its in-tile neighbours q to
+// min(value, mask[q]) when that is higher (a compare-and-swap on the packed
+// word, lanes may share a word) and newly raised pixels are queued, placed
+// by ballot and population count.  Every update is a valid monotone step of
+// the propagation rule (MR.cu:43-44) and the queue empties only when no
+// queued pixel can raise a neighbour, so the tile ends at its fixed point.
+// Returns false (the caller finishes the tile with passes over every row)
+// when the FIFO would overflow or a bound is reached; what was raised stands.
+// `rows_chg` (per lane) collects the rows that rose (bit r - 1), `col_now`
+// whether the tile's first / last pixel column rose.
+template <int DT>
+__device__ __forceinline__ uint32_t pq_get(const uint32_t* words, int r, int c) {
+    using P = Px<DT>;
+    const uint32_t w = *(const volatile uint32_t*)&words[r * 32 + c / P::PPW];
+    constexpr int B = 8 * P::BPP;
+    return B == 32 ? w : (w >> (B * (c % P::PPW))) & ((1u << B) - 1u);
+}
+
+// Raises pixel (r, c) of `words` to v when v is higher; true when this lane
+// raised it.  *fail is set when the compare-and-swap loop gives up.
+template <int DT>
+__device__ __forceinline__ bool pq_raise(uint32_t* words, int r, int c, uint32_t v, bool* fail) {
+    using P = Px<DT>;
+    uint32_t* w = &words[r * 32 + c / P::PPW];
+    if (DT == DT_I32) return atomicMax(reinterpret_cast<int*>(w), (int)v) < (int)v;
+    constexpr int B = 8 * P::BPP;
+    const int sh = B * (c % P::PPW);
+    const uint32_t msk = ((1u << B) - 1u) << sh;
+    uint32_t old = *(volatile uint32_t*)w;
+    for (int it = 0; it < 64; ++it) {
+        if (((old & msk) >> sh) >= v) return false;
+        const uint32_t got = atomicCAS(w, old, (old & ~msk) | (v << sh));
+        if (got == old) return true;
+        old = got;
+    }
+    *fail = true;
+    return false;
+}
+
+template <int DT, int CONN, int TH>
+__device__ bool pq_solve(WarpSmem<TH>& sm, int lane, unsigned long long& rows_chg, bool& col_now, unsigned& rounds) {
+    using P = Px<DT>;
+    constexpr int TW = 32 * P::PPW;
+    int head = 0, tail = 0;  // warp-uniform
+    bool fail = false;
+    // value of any pixel of rows 0..TH+1, columns -1..TW (halo columns)
+    auto val = [&](int r, int c) -> uint32_t {
+        if (c < 0) return sm.hLm[r];
+        if (c >= TW) return sm.hRm[r];
+        return pq_get<DT>(sm.tm, r, c);
+    };
+    // queue the pixels of the lanes with `want` (warp-uniform call)
+    auto enqueue = [&](bool want, int r, int c) {
+        const unsigned b = __ballot_sync(FULL, want);
+        const int n = __popc(b);
+        if (n == 0) return;
+        if (tail - head + n > kPqCap) {
+            fail = true;
+            return;
+        }
+        if (want) {
+            const int rank = __popc(b & ((1u << lane) - 1u));
+            sm.pq[(tail + rank) % kPqCap] = (unsigned short)(r * TW + c);
+        }
+        tail += n;
+    };
+    auto raised = [&](int r, int c) {
+        rows_chg |= 1ull << (r - 1);
+        if (c == 0 || c == TW - 1) col_now = true;
+    };
+    // seeds: the boundary ring (top and bottom rows, first and last columns)
+    constexpr int RING = 2 * TW + 2 * TH;
+    for (int i0 = 0; i0 < RING; i0 += 32) {
+        const int i = i0 + lane;
+        int r = 0, c = 0;
+        bool on = i < RING;
+        if (i < TW) { r = 1; c = i; }
+        else if (i < 2 * TW) { r = TH; c = i - TW; }
+        else if (i < 2 * TW + TH) { r = i - 2 * TW + 1; c = 0; }
+        else { r = i - 2 * TW - TH + 1; c = TW - 1; }
+        bool up = false;
+        if (on) {
+            const uint32_t k = pq_get<DT>(sm.tk, r, c);
+            uint32_t best = P::mx(val(r - 1, c), val(r + 1, c));
+            best = P::mx(best, P::mx(val(r, c - 1), val(r, c + 1)));
+            if (CONN == 8) {
+                best = P::mx(best, P::mx(val(r - 1, c - 1), val(r - 1, c + 1)));
+                best = P::mx(best, P::mx(val(r + 1, c - 1), val(r + 1, c + 1)));
+            }
+            const uint32_t cand = P::mn(best, k);
+            if (P::gt(cand, pq_get<DT>(sm.tm, r, c)) && pq_raise<DT>(sm.tm, r, c, cand, &fail)) {
+                up = true;
+                raised(r, c);
+            }
+        }
+        enqueue(up, r, c);
+        if (__any_sync(FULL, fail)) return false;
+    }
+    // rounds
+    constexpr int DR[8] = {-1, 1, 0, 0, -1, -1, 1, 1};
+    constexpr int DC[8] = {0, 0, -1, 1, -1, 1, -1, 1};
+    while (head != tail) {
+        if (++rounds > 4096u) return false;
+        const int k = min(tail - head, 32);
+        int r = 0, c = 0;
+        uint32_t v = 0u;
+        const bool mine = lane < k;
+        if (mine) {
+            const int p = sm.pq[(head + lane) % kPqCap];
+            r = p / TW;
+            c = p - r * TW;
+            v = pq_get<DT>(sm.tm, r, c);
+        }
+        __syncwarp();
+        head += k;
+#pragma unroll
+        for (int dir = 0; dir < CONN; ++dir) {
+            const int rq = r + DR[dir], cq = c + DC[dir];
+            bool up = false;
+            if (mine && rq >= 1 && rq <= TH && cq >= 0 && cq < TW) {
+                const uint32_t cand = P::mn(v, pq_get<DT>(sm.tk, rq, cq));
+                if (P::gt(cand, pq_get<DT>(sm.tm, rq, cq)) && pq_raise<DT>(sm.tm, rq, cq, cand, &fail)) {
+                    up = true;
+                    raised(rq, cq);
+                }
+            }
+            enqueue(up, rq, cq);
+            if (__any_sync(FULL, fail)) return false;
+        }
+    }
+    return true;
+}
 
 // One warp: fetch tile (tx, ty) of image d with its one-pixel halo, run
 // raster / anti-raster sweeps until a sweep after the first changes nothing,
@@ -873,7 +1026,28 @@ __device__ __forceinline__ VisitResult visit_tile(const ImgDesc& d, int tx, int 
         col_changed = false;
         t_flush += clock64() - f0;
     };
-    if (!early.passes(lane)) {
+    // A revisit by the pixel queue when asked for; if it cannot finish, the
+    // passes take the tile with every row dirty.
+    bool solved = false;
+    bool run_passes = early.passes(lane);
+    if (early.pq() && sides != 0xffu) {
+        unsigned long long rows_chg = 0ull;
+        bool col_now = false;
+        unsigned rounds = 0u;
+        solved = pq_solve<DT, CONN, TH>(sm, lane, rows_chg, col_now, rounds);
+        __syncwarp();
+        const unsigned long long chg = warp_or64(rows_chg);
+        pend_rows |= chg;
+        col_changed |= col_now;
+        res.row_steps += rounds;
+        ++sweeps;
+        if (!solved) {
+            run_passes = true;
+            sides = 0xffu;
+        }
+    }
+    if (solved) {
+    } else if (!run_passes) {
         // Rows whose halo inputs are new are processed by the first two
         // sweeps: the top row by the raster sweep (N, NW, NE), the bottom row
         // by the anti-raster sweep (S, SW, SE), every row when a side column

@@ -190,6 +190,8 @@ constexpr int kCtaKeep = 16;
 struct MutexCtaBuf {
     int lock;
     int n;
+    int taker;    // 1 while one of this CTA's warps works the global stack
+    int waiting;  // this CTA's warps waiting for work
     unsigned e[kCtaBuf];
 };
 __shared__ MutexCtaBuf s_cq;
@@ -325,6 +327,7 @@ struct EarlyFlush {
     int tx, ty;
     WarpCounters* cnt;
     bool use_passes;  // in-tile solver of this visit
+    bool use_pq;      // revisits by the pixel queue
     // Front-bound: more than half of the grid's warps have claimed a ring
     // position that no producer has filled yet (they wait for work).  A
     // quarter or an eighth switches too early on h-dome images, three
@@ -338,6 +341,7 @@ struct EarlyFlush {
         return __shfl_sync(FULL, v, 0) != 0u;
     }
     __device__ bool passes(int) { return use_passes; }
+    __device__ bool pq() { return use_pq; }
     __device__ bool want(int lane) { return sample(*a, lane); }
     __device__ void flush(unsigned nb, int lane) {
         __threadfence();  // release: the rows just stored before the neighbours' DIRTY
@@ -374,14 +378,16 @@ __device__ bool process_entry(const EngineArgs& a, unsigned g, WarpSmem<TH>& sm,
         // In-tile solver: row sweeps (fewest instructions) while the warps
         // are busy, passes (shortest latency) while many wait for work (async
         // queue; the round-based queues use the sweeps unless told otherwise).
-        bool use_passes = a.solver == 2;
+        // Solver 3: revisits by the pixel queue, first visits by passes.
+        bool use_passes = a.solver == 2 || a.solver == 3;
         if (a.solver == 0 && VAR == VAR_ASYNC) use_passes = EarlyFlush<VAR_ASYNC>::sample(a, lane);
+        const bool use_pq = a.solver == 3;
         VisitResult r;
         if (VAR == VAR_ASYNC) {
-            EarlyFlush<VAR> early{&a, &d, tx, ty, &cnt, use_passes};
+            EarlyFlush<VAR> early{&a, &d, tx, ty, &cnt, use_passes, use_pq};
             r = dispatch_visit<TH>(d, tx, ty, sm, lane, phase, a.timeout_ns, sides, early);
         } else {
-            NoEarlyFlush early{use_passes};
+            NoEarlyFlush early{use_passes, use_pq};
             r = dispatch_visit<TH>(d, tx, ty, sm, lane, phase, a.timeout_ns, sides, early);
         }
         if (!r.ok) {
@@ -421,132 +427,169 @@ __device__ bool process_entry(const EngineArgs& a, unsigned g, WarpSmem<TH>& sm,
 }
 
 // ------------------------------------------------------- mutex worker
+// The global stack's side of a take, for the one warp of its CTA that works
+// it: up to kMutexBatch entries under the lock (enough for this CTA's
+// waiting warps, or the stack divided among the CTAs while it is long; the
+// reference takes one, IWPP MP/src/MorphologicalReconstruction.cu:221), the
+// first returned in *g, the rest buffered for the CTA.  Returns 0 with an
+// entry, 1 when the job is over for this warp (finished or an error), 2 when
+// there is nothing to take now.  On overflow the quiescent stack is refilled
+// with every tile (MR.cu:785-806).
+__device__ int mutex_global_take(const EngineArgs& a, int lane, WarpCounters& cnt, unsigned* g) {
+    // Look before queueing for the lock: a ticket only while the stack holds
+    // more entries than there are warps in line (a ticket lock serves in
+    // arrival order, so warps queued for an empty stack would delay every
+    // warp that inserts), or when the job looks finished but an overflow
+    // needs the refill.  A finished job (nothing stacked or pending, no
+    // overflow) is left without the lock.
+    int look = 0;  // 0 back off, 1 take a ticket, 2 finished
+    if (lane == 0) {
+        const int top = ld_volatile(&a.ctrl->top);
+        const int pend = ld_volatile(&a.ctrl->pending);
+        const unsigned line = ld_volatile(&a.ctrl->lock_next) - ld_volatile(&a.ctrl->lock_serving);
+        if (pend == 0 && top == 0 && ld_volatile(&a.ctrl->overflow) == 0u)
+            look = 2;
+        else if (top > (int)line || pend == 0)
+            look = 1;
+    }
+    look = __shfl_sync(FULL, look, 0);
+    if (look == 2) return 1;
+    if (look == 0) return 2;
+    int n = 0, base = 0, verdict = 0;  // verdict: 0 entries / nothing, 1 exit, 2 refill
+    unsigned ticket = 0u;
+    if (lane == 0) {
+        if (!mutex_lock(a, &ticket)) {
+            verdict = 1;
+        } else {
+            const int top = ld_volatile(&a.ctrl->top);
+            if (top > 0) {
+                const int want = *(volatile int*)&s_cq.waiting + 1;
+                n = top / (int)gridDim.x;
+                n = n < want ? want : n;
+                n = n > kMutexBatch ? kMutexBatch : n;
+                n = n > top ? top : n;
+                base = top - n;
+            } else if (ld_volatile(&a.ctrl->pending) == 0) {
+                if (ld_volatile(&a.ctrl->overflow) != 0u) {
+                    if ((int)ld_volatile(&a.ctrl->restarts) >= a.max_restarts) {
+                        set_error(a.ctrl, DEV_ERR_OVERFLOW);
+                        verdict = 1;
+                    } else {
+                        verdict = 2;
+                    }
+                } else {
+                    verdict = 1;
+                }
+            }
+            if (n == 0 && verdict != 2) mutex_unlock(a, ticket);
+        }
+    }
+    n = __shfl_sync(FULL, n, 0);
+    base = __shfl_sync(FULL, base, 0);
+    verdict = __shfl_sync(FULL, verdict, 0);
+    if (verdict == 1) return 1;
+    if (verdict == 2) {
+        // quiescent with lost insertions: refill with every tile (lock held)
+        for (unsigned i = (unsigned)lane; i < a.G && i < a.cap; i += 32u) a.q0[i] = a.G - 1u - i;
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) {
+            const int cnt_all = (int)(a.G < a.cap ? a.G : a.cap);
+            atomicAdd(&a.ctrl->pending, cnt_all);
+            atomicExch(&a.ctrl->overflow, 0u);
+            atomicAdd(&a.ctrl->restarts, 1u);
+            *(volatile int*)&a.ctrl->top = cnt_all;
+            mutex_unlock(a, ticket);
+        }
+        __syncwarp();
+        return 2;
+    }
+    if (n == 0) return 2;
+    // copy the taken entries out before the lock is released
+    unsigned mine = 0u;
+    if (lane < n) mine = __ldcg(&a.q0[base + lane]);  // from L2: the slot may have been cached before
+    __syncwarp();
+    if (lane == 0) {
+        *(volatile int*)&a.ctrl->top = base;
+        mutex_unlock(a, ticket);
+    }
+    *g = __shfl_sync(FULL, mine, 0);
+    cta_push(a, lane >= 1 && lane < n, mine, lane, cnt, true);
+    return 0;
+}
+
 // One persistent launch.  A warp takes its next entry from its CTA's buffer;
-// when that is empty, it takes a share of the global LIFO stack under the
-// lock (up to kMutexBatch entries, the stack divided among the CTAs; the
-// reference takes one, IWPP MP/src/MorphologicalReconstruction.cu:221),
-// keeps the first and buffers the rest for its CTA.  Termination: nothing
-// is stacked and no inserted entry is unfinished (`pending` == 0, buffered
-// entries included), which replaces activeBlocksCount
-// (IWPP MP/src/globalQueue.cu:134-145).  On overflow the quiescent stack is
-// refilled with every tile (MR.cu:785-806).
+// when that is empty, one warp of the CTA at a time takes a batch from the
+// global LIFO stack for the CTA (mutex_global_take) while the others wait
+// for it.  Termination: nothing is stacked and no inserted entry is
+// unfinished (`pending` == 0, buffered entries included), which replaces
+// activeBlocksCount (IWPP MP/src/globalQueue.cu:134-145).
 template <int TH>
 __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, WarpCounters& cnt, unsigned& phase) {
     if (threadIdx.x == 0) {
         s_cq.lock = 0;
         s_cq.n = 0;
+        s_cq.taker = 0;
+        s_cq.waiting = 0;
     }
     __syncthreads();
     long long idle_since = 0;
     unsigned idle_progress = 0u;
     unsigned ns = 64;
-    bool idle = false;  // counted in ctrl->idle
+    bool idle = false;  // counted in ctrl->idle and s_cq.waiting
     auto leave_idle = [&]() {
-        if (idle && lane == 0) atomicSub(&a.ctrl->idle, 1u);
+        if (idle && lane == 0) {
+            atomicSub(&a.ctrl->idle, 1u);
+            atomicSub(&s_cq.waiting, 1);
+        }
         idle = false;
     };
     for (;;) {
         if (ld_volatile(&a.ctrl->error) != 0u) break;
         const long long qr0 = clock64();
         unsigned g = cta_take(a, lane);
+        int verdict = 0;  // 0 an entry, 1 exit, 2 nothing now
         if (g == ~0u) {
-            int n = 0, base = 0, verdict = 0;  // verdict: 0 work/retry, 1 exit, 2 refill
-            // Look before queueing for the lock: an idle warp takes a ticket
-            // only while the stack holds more entries than there are warps in
-            // line (a ticket lock serves in arrival order, so idle warps
-            // queued for an empty stack would delay every warp that
-            // inserts), or when the job looks finished but an overflow needs
-            // the refill.  A finished job (no entry in the stack or pending,
-            // no overflow) is left without the lock.
-            int look = 0;  // 0 back off, 1 take a ticket, 2 finished
-            if (lane == 0) {
-                const int top = ld_volatile(&a.ctrl->top);
-                const int pend = ld_volatile(&a.ctrl->pending);
-                const unsigned line = ld_volatile(&a.ctrl->lock_next) - ld_volatile(&a.ctrl->lock_serving);
-                if (pend == 0 && top == 0 && ld_volatile(&a.ctrl->overflow) == 0u)
-                    look = 2;
-                else if (top > (int)line || pend == 0)
-                    look = 1;
-            }
-            look = __shfl_sync(FULL, look, 0);
-            if (look == 2) break;
-            unsigned ticket = 0u;
-            if (lane == 0 && look == 1) {
-                if (!mutex_lock(a, &ticket)) {
-                    verdict = 1;
-                } else {
-                    const int top = ld_volatile(&a.ctrl->top);
-                    if (top > 0) {
-                        // the stack divided among the CTAs, at most a batch
-                        n = top / (int)gridDim.x;
-                        n = n < 1 ? 1 : n > kMutexBatch ? kMutexBatch : n;
-                        base = top - n;
-                    } else if (ld_volatile(&a.ctrl->pending) == 0) {
-                        if (ld_volatile(&a.ctrl->overflow) != 0u) {
-                            if ((int)ld_volatile(&a.ctrl->restarts) >= a.max_restarts) {
-                                set_error(a.ctrl, DEV_ERR_OVERFLOW);
-                                verdict = 1;
-                            } else {
-                                verdict = 2;
-                            }
-                        } else {
-                            verdict = 1;
-                        }
-                    }
-                    if (n == 0 && verdict != 2) mutex_unlock(a, ticket);
-                }
-            }
-            n = __shfl_sync(FULL, n, 0);
-            base = __shfl_sync(FULL, base, 0);
-            verdict = __shfl_sync(FULL, verdict, 0);
-            if (verdict == 1) break;
-            if (verdict == 2) {
-                // quiescent with lost insertions: refill with every tile (lock held)
-                for (unsigned i = (unsigned)lane; i < a.G && i < a.cap; i += 32u) a.q0[i] = a.G - 1u - i;
+            int taker = 0;
+            if (lane == 0) taker = atomicCAS(&s_cq.taker, 0, 1) == 0 ? 1 : 0;
+            taker = __shfl_sync(FULL, taker, 0);
+            if (taker) {
+                verdict = mutex_global_take(a, lane, cnt, &g);
                 __syncwarp();
+                if (lane == 0) atomicExch(&s_cq.taker, 0);
+            } else {
+                // another warp of this CTA is at the global stack: wait for
+                // its batch, leaving when the job is over
+                int over = 0;
+                if (lane == 0)
+                    over = ld_volatile(&a.ctrl->pending) == 0 && ld_volatile(&a.ctrl->top) == 0 &&
+                           ld_volatile(&a.ctrl->overflow) == 0u;
+                verdict = __shfl_sync(FULL, over, 0) ? 1 : 2;
+            }
+        }
+        if (verdict == 1) break;
+        if (verdict == 2) {
+            // nothing to take but work in flight: back off, bounded by progress
+            if (!idle) {
                 if (lane == 0) {
-                    const int cnt_all = (int)(a.G < a.cap ? a.G : a.cap);
-                    atomicAdd(&a.ctrl->pending, cnt_all);
-                    atomicExch(&a.ctrl->overflow, 0u);
-                    atomicAdd(&a.ctrl->restarts, 1u);
-                    __threadfence();
-                    *(volatile int*)&a.ctrl->top = cnt_all;
-                    mutex_unlock(a, ticket);
+                    atomicAdd(&a.ctrl->idle, 1u);
+                    atomicAdd(&s_cq.waiting, 1);
                 }
-                __syncwarp();
-                continue;
+                idle = true;
             }
-            if (n == 0) {
-                // nothing to take but work in flight: back off, bounded by progress
-                if (!idle) {
-                    if (lane == 0) atomicAdd(&a.ctrl->idle, 1u);
-                    idle = true;
-                }
-                const unsigned prog = ld_volatile(&a.ctrl->progress);
-                const long long now = globaltimer_ns();
-                if (idle_since == 0 || prog != idle_progress) {
-                    idle_since = now;
-                    idle_progress = prog;
-                } else if (now - idle_since > a.timeout_ns) {
-                    if (lane == 0) set_error(a.ctrl, DEV_ERR_TIMEOUT);
-                    break;
-                }
-                __nanosleep(ns);
-                if (ns < 2048) ns <<= 1;
-                cnt.phase[0] += clock64() - qr0;
-                continue;
+            const unsigned prog = ld_volatile(&a.ctrl->progress);
+            const long long now = globaltimer_ns();
+            if (idle_since == 0 || prog != idle_progress) {
+                idle_since = now;
+                idle_progress = prog;
+            } else if (now - idle_since > a.timeout_ns) {
+                if (lane == 0) set_error(a.ctrl, DEV_ERR_TIMEOUT);
+                break;
             }
-            // copy the taken entries out before the lock is released: the
-            // first is this warp's, the rest go to the CTA's buffer
-            unsigned mine = 0u;
-            if (lane < n) mine = __ldcg(&a.q0[base + lane]);  // from L2: the slot may have been cached before
-            __syncwarp();
-            if (lane == 0) {
-                *(volatile int*)&a.ctrl->top = base;
-                mutex_unlock(a, ticket);
-            }
-            g = __shfl_sync(FULL, mine, 0);
-            cta_push(a, lane >= 1 && lane < n, mine, lane, cnt, true);
+            __nanosleep(ns);
+            if (ns < 2048) ns <<= 1;
+            cnt.phase[0] += clock64() - qr0;
+            continue;
         }
         leave_idle();
         idle_since = 0;
@@ -571,7 +614,8 @@ __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
         }
         // share: the global stack is empty while warps elsewhere wait
         int share = 0;
-        if (lane == 0 && cq_count() >= 2 && ld_volatile(&a.ctrl->top) == 0 && ld_volatile(&a.ctrl->idle) > 0u)
+        if (lane == 0 && cq_count() >= 2 && ld_volatile(&a.ctrl->top) == 0 &&
+            ld_volatile(&a.ctrl->idle) > (unsigned)*(volatile int*)&s_cq.waiting)
             share = 1;
         if (__shfl_sync(FULL, share, 0)) cta_spill(a, lane, __shfl_sync(FULL, cq_count(), 0) / 2);
     }

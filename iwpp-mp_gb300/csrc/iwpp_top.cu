@@ -706,43 +706,60 @@ __global__ void seed_kernel(const ImgDesc d, unsigned* state, unsigned* list, un
     }
 }
 
-// The same check with 16-byte lanes: a warp covers four engine tiles side by
-// side (8 lanes each, 512 bytes of a row), the words of a lane updated with
-// byte / half-word SIMD, the side neighbours of a word's pixels by funnel
-// shifts of the adjacent words, and rows loaded kSeedAhead ahead into a
-// register ring.  Rows must start on 16-byte boundaries (both planes).
+// The same check with wide lanes: a lane holds WPL words (8 or 16 bytes) of
+// a row, so a warp covers WPL engine tiles side by side (32 / WPL lanes
+// each); the words are updated with byte / half-word SIMD, the side
+// neighbours of a word's pixels come from funnel shifts of the adjacent
+// words, and rows are loaded kSeedAhead ahead into a register ring.  Rows
+// must start on 16-byte boundaries (both planes).  Eight-byte lanes keep
+// the registers per thread low enough for eight CTAs per SM.
 constexpr int kSeedAhead = 2;
 constexpr int kSeedThreads = 128;
+constexpr int kSeedWords = 2;  // words per lane
 
-// 16 bytes of row y from byte b0 (pixels past the row or outside the image:
+// WPL words of row y from byte b0 (pixels past the row or outside the image:
 // the least value).
-template <int DT>
-__device__ __forceinline__ uint4 seed_load16(const ImgDesc& d, const unsigned char* base, long long pitch, int y,
-                                             long long b0, long long row_bytes) {
+template <int DT, int WPL>
+__device__ __forceinline__ void seed_load(const ImgDesc& d, const unsigned char* base, long long pitch, int y,
+                                          long long b0, long long row_bytes, uint32_t (&w)[WPL]) {
     using P = Px<DT>;
-    uint4 v = make_uint4(P::MINW, P::MINW, P::MINW, P::MINW);
-    if (y < 0 || y >= d.H || b0 >= row_bytes) return v;
-    const unsigned char* p = base + (size_t)y * pitch + b0;
-    if (b0 + 16 <= row_bytes) return __ldg(reinterpret_cast<const uint4*>(p));
-    uint32_t w[4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const long long b = b0 + 4 * i;
-        w[i] = b < row_bytes ? load_word_plain<DT>(p + 4 * i, (int)((row_bytes - b) / P::BPP), false) : P::MINW;
+    for (int i = 0; i < WPL; ++i) w[i] = P::MINW;
+    if (y < 0 || y >= d.H || b0 >= row_bytes) return;
+    const unsigned char* p = base + (size_t)y * pitch + b0;
+    if (b0 + 4 * WPL <= row_bytes) {
+        if constexpr (WPL == 4) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
+            w[0] = v.x;
+            w[1] = v.y;
+            w[2] = v.z;
+            w[3] = v.w;
+        } else {
+            const uint2 v = __ldg(reinterpret_cast<const uint2*>(p));
+            w[0] = v.x;
+            w[1] = v.y;
+        }
+        return;
     }
-    return make_uint4(w[0], w[1], w[2], w[3]);
+#pragma unroll
+    for (int i = 0; i < WPL; ++i) {
+        const long long b = b0 + 4 * i;
+        if (b < row_bytes) w[i] = load_word_plain<DT>(p + 4 * i, (int)((row_bytes - b) / P::BPP), false);
+    }
 }
 
-template <int DT>
-__global__ void __launch_bounds__(kSeedThreads, 4)
-    seed16_kernel(const ImgDesc d, unsigned* state, unsigned* list, unsigned* nlist) {
+template <int DT, int WPL>
+__global__ void __launch_bounds__(kSeedThreads, 8)
+    seed_wide_kernel(const ImgDesc d, unsigned* state, unsigned* list, unsigned* nlist) {
+    static_assert(WPL == 2 || WPL == 4, "8- or 16-byte lanes");
     if (gated_off(d)) return;
     using P = Px<DT>;
     constexpr int BITS = 8 * P::BPP;  // bits per pixel
     constexpr int TW = 32 * P::PPW;   // pixels per engine tile row
+    constexpr int LPT = 32 / WPL;     // lanes per tile
     const int lane = threadIdx.x & 31;
-    const int q = lane >> 3;          // this lane's tile of the four
-    const int gx_n = (d.tiles_x + 3) / 4;
+    const int q = lane / LPT;         // this lane's tile of the WPL
+    const int gx_n = (d.tiles_x + WPL - 1) / WPL;
     const long long units = (long long)gx_n * d.tiles_y;
     const long long wg = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
@@ -751,27 +768,32 @@ __global__ void __launch_bounds__(kSeedThreads, 4)
     for (long long unit = wg; unit < units; unit += nw) {
         const int ty = (int)(unit / gx_n), gx = (int)(unit - (long long)ty * gx_n);
         const int y0 = ty * TH, rows = min(TH, d.H - y0);
-        const long long b0 = (long long)gx * 512 + lane * 16;
-        const int xl = gx * 4 * TW - 1, xr = (gx + 1) * 4 * TW;  // halo columns
+        const long long b0 = (long long)gx * (128 * WPL) + lane * (4 * WPL);
+        const int xl = gx * WPL * TW - 1, xr = (gx + 1) * WPL * TW;  // halo columns
         auto halo = [&](int y) -> uint32_t {
             if (lane == 0) return seed_px<DT>(d, y, xl);
             if (lane == 31) return seed_px<DT>(d, y, xr);
             return P::MINPX;
         };
-        // window: marker rows r - 1, r (words), mask row r, halo pixels
-        uint4 mu = seed_load16<DT>(d, d.marker, d.pitch_m, y0 - 1, b0, row_bytes);
-        uint4 mc = seed_load16<DT>(d, d.marker, d.pitch_m, y0, b0, row_bytes);
-        uint4 kc = seed_load16<DT>(d, d.mask, d.pitch_k, y0, b0, row_bytes);
+        // window: marker rows r - 1, r, mask row r, halo pixels
+        uint32_t mu[WPL], mc[WPL], kc[WPL];
+        seed_load<DT, WPL>(d, d.marker, d.pitch_m, y0 - 1, b0, row_bytes, mu);
+        seed_load<DT, WPL>(d, d.marker, d.pitch_m, y0, b0, row_bytes, mc);
+        seed_load<DT, WPL>(d, d.mask, d.pitch_k, y0, b0, row_bytes, kc);
         uint32_t hu = halo(y0 - 1), hc = halo(y0);
         // ring slot i holds marker / mask / halo of row r + 1 + i
-        uint4 rm[kSeedAhead], rk[kSeedAhead];
+        uint32_t rm[kSeedAhead][WPL], rk[kSeedAhead][WPL];
         uint32_t rh[kSeedAhead];
 #pragma unroll
         for (int i = 0; i < kSeedAhead; ++i) {
             const int y = y0 + 1 + i;
-            rm[i] = seed_load16<DT>(d, d.marker, d.pitch_m, y, b0, row_bytes);
-            rk[i] = i + 1 < rows ? seed_load16<DT>(d, d.mask, d.pitch_k, y, b0, row_bytes)
-                                 : make_uint4(P::MINW, P::MINW, P::MINW, P::MINW);
+            seed_load<DT, WPL>(d, d.marker, d.pitch_m, y, b0, row_bytes, rm[i]);
+            if (i + 1 < rows) {
+                seed_load<DT, WPL>(d, d.mask, d.pitch_k, y, b0, row_bytes, rk[i]);
+            } else {
+#pragma unroll
+                for (int w = 0; w < WPL; ++w) rk[i][w] = P::MINW;
+            }
             rh[i] = halo(y);
         }
         bool mine = false;
@@ -780,50 +802,60 @@ __global__ void __launch_bounds__(kSeedThreads, 4)
             for (int i = 0; i < kSeedAhead; ++i) {
                 const int r = r0 + i;
                 if (r >= rows) break;  // warp-uniform
-                const uint4 md = rm[i], kn = rk[i];
+                uint32_t md[WPL], kn[WPL];
+#pragma unroll
+                for (int w = 0; w < WPL; ++w) {
+                    md[w] = rm[i][w];
+                    kn[w] = rk[i][w];
+                }
                 const uint32_t hd = rh[i];
                 {
                     const int y = y0 + r + 1 + kSeedAhead;
-                    rm[i] = seed_load16<DT>(d, d.marker, d.pitch_m, y, b0, row_bytes);
-                    rk[i] = r + 1 + kSeedAhead < rows ? seed_load16<DT>(d, d.mask, d.pitch_k, y, b0, row_bytes)
-                                                     : make_uint4(P::MINW, P::MINW, P::MINW, P::MINW);
+                    seed_load<DT, WPL>(d, d.marker, d.pitch_m, y, b0, row_bytes, rm[i]);
+                    if (r + 1 + kSeedAhead < rows) {
+                        seed_load<DT, WPL>(d, d.mask, d.pitch_k, y, b0, row_bytes, rk[i]);
+                    } else {
+#pragma unroll
+                        for (int w = 0; w < WPL; ++w) rk[i][w] = P::MINW;
+                    }
                     rh[i] = halo(y);
                 }
-                const uint32_t U[4] = {mu.x, mu.y, mu.z, mu.w}, C[4] = {mc.x, mc.y, mc.z, mc.w};
-                const uint32_t Dn[4] = {md.x, md.y, md.z, md.w}, K[4] = {kc.x, kc.y, kc.z, kc.w};
                 // what a column offers its side neighbours: itself, or with
                 // 8-connectivity the largest of its three rows
-                uint32_t V[4], S[4];
+                uint32_t V[WPL], S[WPL];
 #pragma unroll
-                for (int w = 0; w < 4; ++w) {
-                    V[w] = word_max<DT>(U[w], Dn[w]);
-                    S[w] = d.conn == 8 ? word_max<DT>(V[w], C[w]) : C[w];
+                for (int w = 0; w < WPL; ++w) {
+                    V[w] = word_max<DT>(mu[w], md[w]);
+                    S[w] = d.conn == 8 ? word_max<DT>(V[w], mc[w]) : mc[w];
                 }
                 const uint32_t hs = d.conn == 8 ? P::mx(P::mx(hu, hc), hd) : hc;
-                uint32_t left = __shfl_up_sync(FULL, S[3], 1), right = __shfl_down_sync(FULL, S[0], 1);
+                uint32_t left = __shfl_up_sync(FULL, S[WPL - 1], 1), right = __shfl_down_sync(FULL, S[0], 1);
                 if (lane == 0) left = BITS == 32 ? hs : hs << (32 - BITS);
                 if (lane == 31) right = hs;
 #pragma unroll
-                for (int w = 0; w < 4; ++w) {
+                for (int w = 0; w < WPL; ++w) {
                     // clamped funnel shifts: a shift of 32 (int32) yields the
                     // adjacent word itself
                     const uint32_t lw = __funnelshift_lc(w == 0 ? left : S[w - 1], S[w], BITS);
-                    const uint32_t rw = __funnelshift_rc(S[w], w == 3 ? right : S[w + 1], BITS);
+                    const uint32_t rw = __funnelshift_rc(S[w], w == WPL - 1 ? right : S[w + 1], BITS);
                     const uint32_t best = word_max<DT>(V[w], word_max<DT>(lw, rw));
-                    mine |= word_any_gt<DT>(word_min<DT>(best, K[w]), C[w]);
+                    mine |= word_any_gt<DT>(word_min<DT>(best, kc[w]), mc[w]);
                 }
-                mu = mc;
-                mc = md;
-                kc = kn;
+#pragma unroll
+                for (int w = 0; w < WPL; ++w) {
+                    mu[w] = mc[w];
+                    mc[w] = md[w];
+                    kc[w] = kn[w];
+                }
                 hu = hc;
                 hc = hd;
             }
         }
-        // a tile is bad when one of its 8 lanes saw a pixel to raise
+        // a tile is bad when one of its lanes saw a pixel to raise
         const unsigned bad = __ballot_sync(FULL, mine);
-        const int tx = gx * 4 + q;
-        if ((lane & 7) == 0 && tx < d.tiles_x) {
-            const bool b = ((bad >> (q * 8)) & 0xffu) != 0u;
+        const int tx = gx * WPL + q;
+        if (lane % LPT == 0 && tx < d.tiles_x) {
+            const bool b = ((bad >> (q * LPT)) & (LPT == 32 ? FULL : ((1u << LPT) - 1u))) != 0u;
             const unsigned g = (unsigned)d.tile_base + (unsigned)(ty * d.tiles_x + tx);
             state[g] = b ? (ST_DIRTY | ST_SIDES) : 0u;
             if (b) list[atomicAdd(nlist, 1u)] = g;
@@ -956,16 +988,17 @@ cudaError_t launch_seed(const ImgDesc& d, unsigned* state, unsigned* list, unsig
         ((reinterpret_cast<uintptr_t>(d.marker) | reinterpret_cast<uintptr_t>(d.mask)) & 15u) == 0u &&
         ((d.pitch_m | d.pitch_k) & 15) == 0;
     if (aligned16) {
-        const long long units = (long long)((d.tiles_x + 3) / 4) * d.tiles_y;
+        constexpr int WPL = kSeedWords;
+        const long long units = (long long)((d.tiles_x + WPL - 1) / WPL) * d.tiles_y;
         long long blocks = (units * 32 + kSeedThreads - 1) / kSeedThreads;
-        if (blocks > 152ll * 32) blocks = 152ll * 32;
+        if (blocks > 152ll * 64) blocks = 152ll * 64;
         if (blocks < 1) blocks = 1;
         if (d.dtype == DT_U8)
-            seed16_kernel<DT_U8><<<(unsigned)blocks, kSeedThreads, 0, s>>>(d, state, list, nlist);
+            seed_wide_kernel<DT_U8, WPL><<<(unsigned)blocks, kSeedThreads, 0, s>>>(d, state, list, nlist);
         else if (d.dtype == DT_U16)
-            seed16_kernel<DT_U16><<<(unsigned)blocks, kSeedThreads, 0, s>>>(d, state, list, nlist);
+            seed_wide_kernel<DT_U16, WPL><<<(unsigned)blocks, kSeedThreads, 0, s>>>(d, state, list, nlist);
         else
-            seed16_kernel<DT_I32><<<(unsigned)blocks, kSeedThreads, 0, s>>>(d, state, list, nlist);
+            seed_wide_kernel<DT_I32, WPL><<<(unsigned)blocks, kSeedThreads, 0, s>>>(d, state, list, nlist);
         if (launches) ++*launches;
         return cudaGetLastError();
     }

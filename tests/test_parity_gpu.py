@@ -85,6 +85,39 @@ def test_random_shapes(dt, conn, variant):
         assert np.array_equal(out, ref), (h, w, int((out != ref).sum()))
 
 
+@pytest.mark.parametrize("dt", [0, 1, 2])
+@pytest.mark.parametrize("conn", [4, 8])
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_pixel_queue_solver(dt, conn, variant):
+    # solver 3: revisits by the per-tile pixel queue (first visits by passes);
+    # ragged shapes, both tile heights, h-dome and sparse markers, and the
+    # configuration-1 images (many revisits, some past the queue's capacity,
+    # which fall back to passes)
+    rng = np.random.default_rng(300 + 10 * dt + conn + len(variant))
+    shapes = [(1, 1), (3, 5), (37, 53), (65, 129), (200, 333), (513, 257), (700, 1500)]
+    for i, (h, w) in enumerate(shapes):
+        mask = synth.noise_mask(w, h, dt, 70 + i, 2.0 + i, 3 + 2 * i)
+        if i % 3 == 0:
+            marker = synth.sparse_marker(mask, 17 + i, 0.002)
+        else:
+            marker = synth.hdome_marker(mask, int(rng.integers(5, 120)))
+        ref = oracle.reconstruct(marker, mask, conn)
+        for th in (32, 64):
+            out, st = gpu_reconstruct(marker, mask, conn, variant, iwpp.Config.make(solver=3, tile_rows=th))
+            assert st.status == 0
+            assert np.array_equal(out, ref), (h, w, th, int((out != ref).sum()))
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_pixel_queue_solver_config1(cfg1, variant):
+    mask, cases = cfg1
+    for case in synth.CONFIG1_CASES:
+        marker, ref = cases[case]
+        out, st = gpu_reconstruct(marker, mask, case[0], variant, iwpp.Config.make(solver=3))
+        assert st.status == 0
+        assert np.array_equal(out, ref), (case, int((out != ref).sum()))
+
+
 @pytest.mark.parametrize("plain", [0, 1])
 @pytest.mark.parametrize("variant", VARIANTS)
 def test_tma_and_plain_load_paths_agree(plain, variant):
