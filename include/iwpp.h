@@ -78,7 +78,7 @@ typedef struct iwpp_config {
                                   queue in shared memory (first visits by passes) */
     int front_passes;          /* the front stage: the pixels at the mask's largest value
                                   raised by connected-component labelling, init_passes
-                                  whole-image passes (default 4), and the tile engine started
+                                  whole-image passes (default 2), and the tile engine started
                                   from the tiles still holding a pixel a neighbour can raise:
                                   0 = default (the tuning table's choice, else 3 when the job's
                                   largest image has 2^26 pixels or more and 2 below that),
@@ -87,7 +87,9 @@ typedef struct iwpp_config {
                                   front, and fewer than one tile in 64 with a pixel a neighbour
                                   can raise (a few sparse seeds: long propagation paths) takes
                                   the stage, more leaves the job to the engine (seeded from that
-                                  check) */
+                                  check), 4 = the seed check alone: the engine starts from the
+                                  tiles holding a pixel a neighbour can raise instead of every
+                                  tile (no labelling, no passes) */
     int phantom_work;          /* fault-injection hook for tests, 0 normally.  1: the job counts
                                   one unit of work that never arrives (a queue entry nobody
                                   inserts; for the round-based queues a CTA that never reaches
@@ -209,7 +211,7 @@ typedef struct iwpp_tune_result {
     iwpp_config best;  /* fastest configuration */
     double best_ms;    /* its median device time */
     double default_ms; /* median device time of the untuned default (default tile height, automatic
-                          solver; front_passes 3 with 4 passes for images of 2^26 pixels or more) */
+                          solver; front_passes 3 with 2 passes for images of 2^26 pixels or more) */
     int candidates;    /* configurations timed */
     int reserved;
 } iwpp_tune_result;

@@ -75,7 +75,7 @@ Config resolve_config(const iwpp_config* c) {
     r.clip_marker = c ? c->clip_marker : 0;
     r.plain_loads = c ? c->plain_loads : 0;
     r.solver = c && c->solver >= 0 && c->solver <= 3 ? c->solver : 0;
-    r.front_passes = c && c->front_passes >= 0 && c->front_passes <= 3 ? c->front_passes : 0;
+    r.front_passes = c && c->front_passes >= 0 && c->front_passes <= 4 ? c->front_passes : 0;
     r.phantom_work = c && c->phantom_work == 1 ? 1 : 0;
     r.dflt_tile = r.tile_rows == 0;
     r.dflt_queue = r.queue_capacity == 0;
@@ -224,9 +224,10 @@ Layout layout_for(long long n_imgs, long long G, long long cap, bool two_queues,
 }
 
 // Whole-image passes after the top-level stage when the caller leaves
-// init_passes at its default: measured on the 16384^2 spiral, four leave
-// about a fifth of the tiles to the engine and two or eight cost more.
-constexpr int kFrontFullPasses = 4;
+// init_passes at its default: measured on the 16384^2 spirals (uint8 /
+// uint16 / int32, ms), 1: 4.02 / 7.30 / 12.31, 2: 3.62 / 6.73 / 10.18,
+// 3: 3.67 / 7.17 / 10.46, 4: 4.13 / 8.10 / 11.74.
+constexpr int kFrontFullPasses = 2;
 // Untuned jobs whose largest image has at least this many pixels decide on
 // the device whether to take the front stage (front_passes 3): the seed
 // check over the untouched images measures the initial front, and a small
@@ -241,6 +242,9 @@ constexpr long long kFrontDefaultPixels = 1ll << 26;
 
 // The job runs the front stage always (1) or as the device decides (3).
 bool job_front(const Config& c) { return c.front_passes == 1 || c.front_passes == 3; }
+// The tile engine starts from a seed check's list (the front stage's, or
+// the check alone: 4) instead of every tile.
+bool job_seeded(const Config& c) { return job_front(c) || c.front_passes == 4; }
 
 // Whole-image raster / anti-raster passes a job runs before the engine.
 int job_full_passes(const Config& c) {
@@ -298,6 +302,7 @@ long long job_queue_capacity(const Job& job) {
 Layout job_layout(const Job& job) {
     const bool two = job.variant == IWPP_QUEUE_DOUBLE || job.variant == IWPP_QUEUE_UNIQUE;
     const bool front = job_front(job.cfg);
+    const bool seeded = job_seeded(job.cfg);
     size_t sweep = 0;
     for (const auto& d : job.descs) {
         if (job_full_passes(job.cfg) > 0) {
@@ -307,7 +312,7 @@ Layout job_layout(const Job& job) {
         }
         if (front) sweep = std::max(sweep, top_scratch_bytes(d));
     }
-    return layout_for((long long)job.descs.size(), job.G, job_queue_capacity(job), two, sweep, front);
+    return layout_for((long long)job.descs.size(), job.G, job_queue_capacity(job), two, sweep, seeded);
 }
 
 // How images whose rows are not 4-byte aligned are handled.
@@ -618,11 +623,13 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
     a.solver = job.cfg.solver;
     a.phantom = job.cfg.phantom_work;
     const bool front = job_front(job.cfg) && job.G > 0;
+    const bool seeded = job_seeded(job.cfg) && job.G > 0;
     const bool gated = front && job.cfg.front_passes == 3;
     unsigned* seed_list = reinterpret_cast<unsigned*>(base + l.off_list);
     unsigned* seed_count = seed_list + job.G;
-    if (front) {
+    if (seeded) {
         a.front = 1;
+        a.front_ran = front && !gated ? 1 : 0;
         a.front_gated = gated ? 1 : 0;
         a.init_list = seed_list;
         a.init_count = seed_count;
@@ -694,11 +701,17 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
                 e = launch_sweep(dv, order[dir], s, base + l.off_sweep, &nl);
                 if (e != cudaSuccess) return cuda_status(e);
             }
-    if (front) {
+    if (seeded) {
         // the tile engine starts from the tiles still holding a pixel that a
         // neighbour can raise (a gated job that left the stage out keeps the
-        // list of its first check: the decision emptied it otherwise)
-        if (!gated) e = cudaMemsetAsync(seed_count, 0, sizeof(unsigned), s);
+        // list of its first check: the decision emptied it otherwise); the
+        // error word and top-pixel count of a job without the stage are
+        // zeroed here (the engine's initialisation keeps them)
+        if (!front) {
+            e = cudaMemsetAsync(&a.ctrl->error, 0, sizeof(a.ctrl->error), s);
+            if (e == cudaSuccess) e = cudaMemsetAsync(&a.ctrl->top_pixels, 0, sizeof(a.ctrl->top_pixels), s);
+        }
+        if (!gated && e == cudaSuccess) e = cudaMemsetAsync(seed_count, 0, sizeof(unsigned), s);
         for (size_t i = 0; i < fdescs.size() && e == cudaSuccess; ++i)
             e = launch_seed(fdescs[i], a.state, seed_list, seed_count, s, &nl);
         if (e != cudaSuccess) return cuda_status(e);

@@ -62,14 +62,36 @@ struct WarpCounters {
 // served with a back-off proportional to their place in line, and a
 // wall-clock bound ends in DEV_ERR_TIMEOUT.  A waiter that gives up leaves
 // the error flag set, which ends every other waiter too.
-__device__ bool mutex_lock(const EngineArgs& a, unsigned* ticket) {
+__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+// The mutex stack's entry count and the ticket being served, read without
+// the lock (hints: look-ahead, quiescence).
+__device__ __forceinline__ int stack_top(const Ctrl* c) {
+    return (int)(unsigned)(*(const volatile unsigned long long*)&c->lock_word >> 32);
+}
+__device__ __forceinline__ unsigned lock_serving(const Ctrl* c) {
+    return (unsigned)*(const volatile unsigned long long*)&c->lock_word;
+}
+
+// Acquires the lock; *top is the stack's entry count at the hand-over.
+__device__ bool mutex_lock(const EngineArgs& a, unsigned* ticket, int* top) {
     const unsigned t = atomicAdd(&a.ctrl->lock_next, 1u);
     *ticket = t;
     const long long t0 = globaltimer_ns();
     unsigned spins = 0;
     for (;;) {
-        const unsigned s = ld_acquire(&a.ctrl->lock_serving);
-        if (s == t) return true;
+        const unsigned long long w = ld_acquire64(&a.ctrl->lock_word);
+        const unsigned s = (unsigned)w;
+        if (s == t) {
+            *top = (int)(unsigned)(w >> 32);
+            return true;
+        }
         const unsigned place = t - s;
         __nanosleep(32u * (place < 32u ? place : 32u));
         if ((++spins & 15u) == 0u) {
@@ -82,8 +104,9 @@ __device__ bool mutex_lock(const EngineArgs& a, unsigned* ticket) {
     }
 }
 
-__device__ __forceinline__ void mutex_unlock(const EngineArgs& a, unsigned ticket) {
-    st_release(&a.ctrl->lock_serving, ticket + 1u);
+// Releases the lock, publishing the stack's new entry count with it.
+__device__ __forceinline__ void mutex_unlock(const EngineArgs& a, unsigned ticket, int top) {
+    st_release64(&a.ctrl->lock_word, ((unsigned long long)(unsigned)top << 32) | (unsigned long long)(ticket + 1u));
 }
 
 // ------------------------------------------------------------------ push
@@ -104,15 +127,15 @@ __device__ void mutex_push_global(const EngineArgs& a, bool want, unsigned gn, i
     int base = -1;
     unsigned ticket = 0u;
     if (lane == 0) {
-        if (mutex_lock(a, &ticket)) {
-            const int top = ld_volatile(&a.ctrl->top);
+        int top = 0;
+        if (mutex_lock(a, &ticket, &top)) {
             if ((unsigned)top + (unsigned)n <= a.cap) {
                 base = top;
                 if (!counted) atomicAdd(&a.ctrl->pending, n);  // before the entries can be taken
             } else {
                 atomicExch(&a.ctrl->overflow, 1u);
                 if (counted) atomicSub(&a.ctrl->pending, n);  // lost: the restart recovers the tiles
-                mutex_unlock(a, ticket);
+                mutex_unlock(a, ticket, top);
             }
         }
     }
@@ -123,10 +146,7 @@ __device__ void mutex_push_global(const EngineArgs& a, bool want, unsigned gn, i
         __threadfence();  // the entry before the release that publishes it
     }
     __syncwarp();
-    if (lane == 0) {
-        *(volatile int*)&a.ctrl->top = base + n;
-        mutex_unlock(a, ticket);
-    }
+    if (lane == 0) mutex_unlock(a, ticket, base + n);
 }
 
 template <int VAR>
@@ -444,9 +464,9 @@ __device__ int mutex_global_take(const EngineArgs& a, int lane, WarpCounters& cn
     // overflow) is left without the lock.
     int look = 0;  // 0 back off, 1 take a ticket, 2 finished
     if (lane == 0) {
-        const int top = ld_volatile(&a.ctrl->top);
+        const int top = stack_top(a.ctrl);
         const int pend = ld_volatile(&a.ctrl->pending);
-        const unsigned line = ld_volatile(&a.ctrl->lock_next) - ld_volatile(&a.ctrl->lock_serving);
+        const unsigned line = ld_volatile(&a.ctrl->lock_next) - lock_serving(a.ctrl);
         if (pend == 0 && top == 0 && ld_volatile(&a.ctrl->overflow) == 0u)
             look = 2;
         else if (top > (int)line || pend == 0)
@@ -457,11 +477,11 @@ __device__ int mutex_global_take(const EngineArgs& a, int lane, WarpCounters& cn
     if (look == 0) return 2;
     int n = 0, base = 0, verdict = 0;  // verdict: 0 entries / nothing, 1 exit, 2 refill
     unsigned ticket = 0u;
+    int top = 0;
     if (lane == 0) {
-        if (!mutex_lock(a, &ticket)) {
+        if (!mutex_lock(a, &ticket, &top)) {
             verdict = 1;
         } else {
-            const int top = ld_volatile(&a.ctrl->top);
             if (top > 0) {
                 const int want = *(volatile int*)&s_cq.waiting + 1;
                 n = top / (int)gridDim.x;
@@ -481,7 +501,7 @@ __device__ int mutex_global_take(const EngineArgs& a, int lane, WarpCounters& cn
                     verdict = 1;
                 }
             }
-            if (n == 0 && verdict != 2) mutex_unlock(a, ticket);
+            if (n == 0 && verdict != 2) mutex_unlock(a, ticket, top);
         }
     }
     n = __shfl_sync(FULL, n, 0);
@@ -498,8 +518,7 @@ __device__ int mutex_global_take(const EngineArgs& a, int lane, WarpCounters& cn
             atomicAdd(&a.ctrl->pending, cnt_all);
             atomicExch(&a.ctrl->overflow, 0u);
             atomicAdd(&a.ctrl->restarts, 1u);
-            *(volatile int*)&a.ctrl->top = cnt_all;
-            mutex_unlock(a, ticket);
+            mutex_unlock(a, ticket, cnt_all);
         }
         __syncwarp();
         return 2;
@@ -508,11 +527,9 @@ __device__ int mutex_global_take(const EngineArgs& a, int lane, WarpCounters& cn
     // copy the taken entries out before the lock is released
     unsigned mine = 0u;
     if (lane < n) mine = __ldcg(&a.q0[base + lane]);  // from L2: the slot may have been cached before
-    __syncwarp();
-    if (lane == 0) {
-        *(volatile int*)&a.ctrl->top = base;
-        mutex_unlock(a, ticket);
-    }
+    // (the vote needs every lane's value: the loads are done before the release)
+    __ballot_sync(FULL, mine == ~0u);
+    if (lane == 0) mutex_unlock(a, ticket, base);
     *g = __shfl_sync(FULL, mine, 0);
     cta_push(a, lane >= 1 && lane < n, mine, lane, cnt, true);
     return 0;
@@ -562,7 +579,7 @@ __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
                 // its batch, leaving when the job is over
                 int over = 0;
                 if (lane == 0)
-                    over = ld_volatile(&a.ctrl->pending) == 0 && ld_volatile(&a.ctrl->top) == 0 &&
+                    over = ld_volatile(&a.ctrl->pending) == 0 && stack_top(a.ctrl) == 0 &&
                            ld_volatile(&a.ctrl->overflow) == 0u;
                 verdict = __shfl_sync(FULL, over, 0) ? 1 : 2;
             }
@@ -614,7 +631,7 @@ __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
         }
         // share: the global stack is empty while warps elsewhere wait
         int share = 0;
-        if (lane == 0 && cq_count() >= 2 && ld_volatile(&a.ctrl->top) == 0 &&
+        if (lane == 0 && cq_count() >= 2 && stack_top(a.ctrl) == 0 &&
             ld_volatile(&a.ctrl->idle) > (unsigned)*(volatile int*)&s_cq.waiting)
             share = 1;
         if (__shfl_sync(FULL, share, 0)) cta_spill(a, lane, __shfl_sync(FULL, cq_count(), 0) / 2);
@@ -861,8 +878,7 @@ __global__ void engine_init_kernel(EngineArgs a, int variant) {
         c->bar_gen = 0u;
         if (!a.front) c->error = 0u;  // else the front passes' error stands
         c->lock_next = 0u;
-        c->lock_serving = 0u;
-        c->top = (int)(n0 < a.cap ? n0 : a.cap);
+        c->lock_word = (unsigned long long)(n0 < a.cap ? n0 : a.cap) << 32;  // ticket 0 served
         c->pending = (int)(n0 < a.cap ? n0 : a.cap);
         c->progress = 0u;
         c->idle = 0u;
@@ -880,7 +896,7 @@ __global__ void engine_init_kernel(EngineArgs a, int variant) {
         c->row_steps = 0ull;
         for (int i = 0; i < 5; ++i) c->phase[i] = 0ull;
         if (!a.front) c->top_pixels = 0ull;  // else the top-level stage's count stands
-        if (!a.front_gated) c->front_gate = a.front ? 1u : 0u;  // else the device's decision stands
+        if (!a.front_gated) c->front_gate = a.front_ran ? 1u : 0u;  // else the device's decision stands
     }
 }
 
@@ -913,8 +929,7 @@ __global__ void queue_test_init_kernel(EngineArgs a, QueueTest t) {
         c->overflow = 0u;
         c->error = 0u;
         c->lock_next = 0u;
-        c->lock_serving = 0u;
-        c->top = 0;
+        c->lock_word = 0ull;
         c->pending = 0;
         c->atail = a.G;  // ring positions below G are the (absent) initial tiles
         t.out[0] = 0ull;
@@ -943,7 +958,7 @@ __global__ void queue_test_insert_kernel(EngineArgs a, int copies) {
 __global__ void queue_test_count_kernel(EngineArgs a, int variant, QueueTest t) {
     const Ctrl* c = a.ctrl;
     unsigned n;
-    if (variant == VAR_MUTEX) n = (unsigned)c->top;
+    if (variant == VAR_MUTEX) n = (unsigned)stack_top(c);
     else if (variant == VAR_ASYNC) n = c->atail - a.G;
     else n = c->wn;
     if (n > a.cap) n = a.cap;

@@ -53,9 +53,11 @@ struct Ctrl {
     unsigned bar_count;
     unsigned bar_gen;
     unsigned error;
-    unsigned lock_next;     // mutex stack: ticket lock (next ticket, ticket being served)
-    unsigned lock_serving;
-    int top;
+    unsigned lock_next;  // mutex stack: the ticket lock's next ticket
+    // mutex stack: the ticket being served (low half) and the number of
+    // stacked entries (high half) in one word, so a hand-over publishes the
+    // stack's top with the lock and the next holder reads both in one load
+    unsigned long long lock_word;
     int pending;        // mutex: entries in the stack or taken and unfinished
     unsigned progress;  // finished entries (for the no-progress timeout)
     unsigned ahead;     // async ring: next position to claim
@@ -84,7 +86,8 @@ struct EngineArgs {
     int max_restarts;
     int solver;  // 0 automatic, 1 row sweeps, 2 passes
     int phantom;  // test hook: one unit of work that never arrives (every wait runs out)
-    int front;    // the front stage (or its seed check) ran before this job's engine launch
+    int front;    // a seed check listed the tiles this job's engine starts from
+    int front_ran;    // the front stage ran (not gated)
     int front_gated;  // the device decided whether the stage ran (Ctrl::front_gate)
     // After front passes: the tiles to start from (ids) and their count (a
     // device counter); nullptr: every tile, in id order.  The tile states

@@ -58,7 +58,7 @@ namespace {
 bool valid_entry(const TuneEntry& e) {
     return (e.tile_rows == 32 || e.tile_rows == 64) && e.solver >= 0 && e.solver <= 3 && e.init_passes >= 0 &&
            e.init_passes <= 64 && e.queue_mult >= 0 && e.queue_mult <= 1024 && e.front_passes >= 0 &&
-           e.front_passes <= 2;
+           e.front_passes <= 3;
 }
 }  // namespace
 

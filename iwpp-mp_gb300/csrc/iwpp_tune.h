@@ -24,13 +24,13 @@ struct TuneEntry {
     int solver;      // 0 / 1 / 2
     int init_passes;
     int queue_mult;  // queue capacity in tiles per tile of the job; 0 = the variant's default
-    int front_passes;  // 0 = no front stage, 1 = the front stage always, 2 = decided on the device
+    int front_passes;  // 0 = no front stage, 1 = always, 2 = decided on the device, 3 = the seed check alone
 };
 
-// iwpp_config.front_passes (1 always, 2 never, 3 decided on the device) of a
-// table entry's front_passes, and back.
-inline int tune_front_code(int stored) { return stored == 1 ? 1 : stored == 2 ? 3 : 2; }
-inline int tune_front_store(int code) { return code == 1 ? 1 : code == 3 ? 2 : 0; }
+// iwpp_config.front_passes (1 always, 2 never, 3 decided on the device, 4 the
+// seed check alone) of a table entry's front_passes, and back.
+inline int tune_front_code(int stored) { return stored == 1 ? 1 : stored == 2 ? 3 : stored == 3 ? 4 : 2; }
+inline int tune_front_store(int code) { return code == 1 ? 1 : code == 3 ? 2 : code == 4 ? 3 : 0; }
 
 int resolve_queue_variant(int variant);  // iwpp_api.cu: IWPP_QUEUE_DEFAULT -> the variant used
 TuneKey tune_key(int variant, const int* dtypes, const int* conns, const long long* pixels, int n);

@@ -52,9 +52,9 @@ def test_front_random_shapes(dt, conn, variant):
         out, st = run(marker, mask, conn, variant)
         assert st.status == 0
         assert np.array_equal(out, ref), (h, w, int((out != ref).sum()))
-        # the top-level stage (6 kernels), four whole-image passes, the seed
+        # the top-level stage (6 kernels), two whole-image passes, the seed
         # check and the engine ran
-        assert st.launches >= 6 + 16 + 3 and st.front_stage == 1
+        assert st.launches >= 6 + 8 + 3 and st.front_stage == 1
         # decided on the device: on images this small an initial front is
         # large against the tile count (or empty), so the stage is left out
         # and the engine starts from the first seed check's list
@@ -64,6 +64,10 @@ def test_front_random_shapes(dt, conn, variant):
         if st.front_stage == 0:
             assert st.top_pixels == 0
             decided_off += 1
+        # the seed check alone: the engine starts from the tiles it lists
+        out, st = run(marker, mask, conn, variant, front_passes=4)
+        assert st.status == 0 and st.front_stage == 0 and st.top_pixels == 0
+        assert np.array_equal(out, ref), (h, w, "seeded", int((out != ref).sum()))
     assert decided_off == len(shapes)
 
 

@@ -28,7 +28,8 @@ def test_table_round_trip(tmp_path):
     p = tmp_path / "t.txt"
     # variant dtype conn pxclass batch tile_rows solver init_passes queue_mult [front_passes]
     # (a v1 line without the last field, a v2 line with it)
-    # (the last field: 0 no front stage, 1 always, 2 decided on the device)
+    # (the last field: 0 no front stage, 1 always, 2 decided on the device,
+    # 3 the seed check alone)
     _write(p, ["3 0 8 24 0 32 1 0 0", "0 1 4 20 1 64 2 1 16 1", "2 0 8 28 0 64 0 4 0 2"])
     iwpp.tune_load(str(p))
     assert iwpp.tune_entries() == 3
@@ -56,7 +57,7 @@ def test_malformed_table_changes_nothing(tmp_path):
     good = tmp_path / "good.txt"
     _write(good, ["3 0 8 24 0 64 0 0 0"])
     iwpp.tune_load(str(good))
-    for bad_line in ["3 0 8 24 0 48 0 0 0", "3 0 8 24 0 64 7 0 0", "3 0 8", "x y z", "3 0 8 24 0 64 0 0 0 3",
+    for bad_line in ["3 0 8 24 0 48 0 0 0", "3 0 8 24 0 64 7 0 0", "3 0 8", "x y z", "3 0 8 24 0 64 0 0 0 4",
                      "3 0 8 24 0 64 0 0 0 1 9"]:
         bad = tmp_path / "bad.txt"
         _write(bad, ["3 1 8 20 0 32 1 0 0", bad_line])
