@@ -270,9 +270,8 @@ IWPP_API int iwpp_sweep_timing(void *marker, const void *mask, size_t pitch_mark
  * 64-row tiles, plain loads; synchronous on `stream` (NULL = legacy default
  * stream).  The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress) and the engine's launch shape with that device
- * current; make that first call before any stream capture.  Both are kept
- * until the process exits, so a cudaDeviceReset between calls is not
- * supported (the kept address would be stale).  All calls share the one
+ * current.  Both are kept until the process exits, so a cudaDeviceReset
+ * between calls is not supported (the kept address would be stale).  All calls share the one
  * array: calls whose work overlaps on the GPU (concurrent host threads or
  * streams) race and must be serialised by the caller.  Each call clears the
  * state it needs; the array otherwise keeps the last call's contents. */
@@ -298,7 +297,8 @@ typedef struct iwpp_server_config {
     int max_batch;             /* requests per batch, 0 = 256 */
     int max_pending;           /* waiting requests before submit says BUSY, 0 = 65536 */
     int variant;               /* queue variant, IWPP_QUEUE_DEFAULT = async */
-    int tile_rows;             /* 0 = default; batches run the tile engine alone (front_passes 2) */
+    int tile_rows;             /* 0 = default; batches start the tile engine from a seed check
+                                  (front_passes 4) */
     int lane_ctas;             /* CTAs per batch launch, 0 = the whole GPU */
     int timeout_ms;            /* device wait bound per batch, 0 = 60000 */
     long long memory_budget;   /* device bytes for admitted requests, 0 = half the free memory at creation */

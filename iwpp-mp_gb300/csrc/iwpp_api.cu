@@ -631,8 +631,17 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
         a.front = 1;
         a.front_ran = front && !gated ? 1 : 0;
         a.front_gated = gated ? 1 : 0;
-        a.init_list = seed_list;
-        a.init_count = seed_count;
+        if (front) {
+            // after the front stage few tiles are left: the engine starts
+            // from the list
+            a.init_list = seed_list;
+            a.init_count = seed_count;
+        } else {
+            // the check alone: its tile states, the queue in tile order
+            // (a list filled by atomics would lose the raster order that
+            // lets a tile's upper and left neighbours go first)
+            a.states_set = 1;
+        }
     }
 
     cudaError_t e = cudaSuccess;
@@ -679,8 +688,8 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
         if (e == cudaSuccess) e = cudaMemsetAsync(&c->top_pixels, 0, sizeof(c->top_pixels), s);
         if (gated) {
             if (e == cudaSuccess) e = cudaMemsetAsync(seed_count, 0, sizeof(unsigned), s);
-            for (size_t i = 0; i < job.descs.size() && e == cudaSuccess; ++i)
-                e = launch_seed(job.descs[i], a.state, seed_list, seed_count, s, &nl);
+            if (e == cudaSuccess)
+                e = launch_seed_batch(a.imgs, job.descs, nullptr, a.state, seed_list, seed_count, s, &nl);
             if (e == cudaSuccess) e = launch_front_decide(&c->front_gate, seed_count, (unsigned)job.G, s, &nl);
         }
         for (size_t i = 0; i < fdescs.size() && e == cudaSuccess; ++i)
@@ -712,8 +721,9 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
             if (e == cudaSuccess) e = cudaMemsetAsync(&a.ctrl->top_pixels, 0, sizeof(a.ctrl->top_pixels), s);
         }
         if (!gated && e == cudaSuccess) e = cudaMemsetAsync(seed_count, 0, sizeof(unsigned), s);
-        for (size_t i = 0; i < fdescs.size() && e == cudaSuccess; ++i)
-            e = launch_seed(fdescs[i], a.state, seed_list, seed_count, s, &nl);
+        if (e == cudaSuccess)
+            e = launch_seed_batch(a.imgs, job.descs, gated ? &a.ctrl->front_gate : nullptr, a.state, seed_list,
+                                  seed_count, s, &nl);
         if (e != cudaSuccess) return cuda_status(e);
     }
     e = engine_launch_init(a, job.variant, s);
@@ -1305,6 +1315,13 @@ int iwpp_autotune(iwpp_handle h, const iwpp_image* images, int n, int variant, i
                 c.front_passes = 2;
                 consider(c, !front_default && th == dflt_th && solver == 0);
             }
+        // stage 1b: the best of stage 1 started from a seed check (the tiles
+        // holding a pixel a neighbour can raise) instead of every tile
+        if (best_ms >= 0.0 && best.front_passes == 2) {
+            iwpp_config c = best;
+            c.front_passes = 4;
+            consider(c, false);
+        }
         // stage 2: the front stage (top-level labelling, then 1 / 2 / 3 / 4 / 8
         // whole-image passes, then the engine from the seed check) with the
         // best tile height and solver; long propagation paths want it

@@ -857,7 +857,7 @@ __global__ void engine_init_kernel(EngineArgs a, int variant) {
     unsigned n0 = a.G;
     if (seeded) n0 = min(*(const volatile unsigned*)a.init_count, a.G);
     for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < a.G; g += stride) {
-        if (!seeded) a.state[g] = ST_DIRTY | ST_SIDES;
+        if (!seeded && !a.states_set) a.state[g] = ST_DIRTY | ST_SIDES;
         if (variant == VAR_MUTEX && g < a.cap) a.q0[g] = seeded ? (g < n0 ? a.init_list[g] : 0u) : a.G - 1u - g;
         if ((variant == VAR_DOUBLE || variant == VAR_UNIQUE) && seeded && g < n0 && g < a.cap) a.q0[g] = a.init_list[g];
     }

@@ -86,7 +86,9 @@ struct EngineArgs {
     int max_restarts;
     int solver;  // 0 automatic, 1 row sweeps, 2 passes
     int phantom;  // test hook: one unit of work that never arrives (every wait runs out)
-    int front;    // a seed check listed the tiles this job's engine starts from
+    int front;    // a seed check ran: the job's error word and top-pixel count stand
+    int states_set;   // the seed check set every tile's state: the queue holds every tile in order,
+                      // clean tiles are released at once
     int front_ran;    // the front stage ran (not gated)
     int front_gated;  // the device decided whether the stage ran (Ctrl::front_gate)
     // After front passes: the tiles to start from (ids) and their count (a

@@ -277,11 +277,13 @@ int iwpp_server_create(iwpp_server* out, int device, const iwpp_server_config* c
     s->cfg.init_passes = -1;
     s->cfg.grid_ctas = c.lane_ctas;
     s->cfg.timeout_ms = c.timeout_ms ? c.timeout_ms : 60000;
-    // Batches of independent requests go to the tile engine alone: the front
-    // stage's scratch is not in the lane workspaces sized below (a workspace
-    // that grows mid-stream synchronises the device), and the decision it
-    // makes would be one for the whole mixed batch.
-    s->cfg.front_passes = 2;
+    // Batches of independent requests start the tile engine from a seed
+    // check (the tiles holding a pixel a neighbour can raise; for sparse
+    // markers most tiles hold none) but take no front stage: its scratch is
+    // not in the lane workspaces sized below (a workspace that grows
+    // mid-stream synchronises the device), and its decision would be one
+    // for the whole mixed batch.
+    s->cfg.front_passes = 4;
 
     int prev = 0;
     cudaGetDevice(&prev);
@@ -307,7 +309,8 @@ int iwpp_server_create(iwpp_server* out, int device, const iwpp_server_config* c
     const int th = c.tile_rows ? c.tile_rows : 32;
     const long long max_tiles = std::max(1ll, s->budget / (2ll * 128ll * th));
     const long long ws_bytes =
-        iwpp_workspace_bytes(max_tiles, s->variant, 0) + (long long)s->max_batch * 512ll + 4096ll;
+        iwpp_workspace_bytes(max_tiles, s->variant, 0) + 4ll * (max_tiles + 64) + (long long)s->max_batch * 512ll +
+        4096ll;  // (the seed list: a word per tile and the count)
     s->lanes.resize((size_t)s->lanes_n);
     rc = e == cudaSuccess ? IWPP_OK : IWPP_ERR_CUDA;
     for (int i = 0; i < s->lanes_n && rc == IWPP_OK; ++i) {

@@ -36,6 +36,8 @@
 //      top_apply_label_kernel (a CTA per tile with more): the local
 //      labelling again (the roots are the least pixel indices, so it is the
 //      same), then the same raise.
+#include <vector>
+
 #include "iwpp_engine.cuh"
 #include "iwpp_top.cuh"
 
@@ -748,118 +750,195 @@ __device__ __forceinline__ void seed_load(const ImgDesc& d, const unsigned char*
     }
 }
 
+// One unit of the check: the WPL engine tiles of tile row ty, group gx of
+// image d.  All lanes of the warp.
 template <int DT, int WPL>
-__global__ void __launch_bounds__(kSeedThreads, 8)
-    seed_wide_kernel(const ImgDesc d, unsigned* state, unsigned* list, unsigned* nlist) {
-    static_assert(WPL == 2 || WPL == 4, "8- or 16-byte lanes");
-    if (gated_off(d)) return;
+__device__ __forceinline__ void seed_unit(const ImgDesc& d, int ty, int gx, unsigned* state, unsigned* list,
+                                          unsigned* nlist) {
     using P = Px<DT>;
     constexpr int BITS = 8 * P::BPP;  // bits per pixel
     constexpr int TW = 32 * P::PPW;   // pixels per engine tile row
     constexpr int LPT = 32 / WPL;     // lanes per tile
     const int lane = threadIdx.x & 31;
     const int q = lane / LPT;         // this lane's tile of the WPL
+    const int TH = d.tile_rows;
+    const long long row_bytes = (long long)d.W * P::BPP;
+    const int y0 = ty * TH, rows = min(TH, d.H - y0);
+    const long long b0 = (long long)gx * (128 * WPL) + lane * (4 * WPL);
+    const int xl = gx * WPL * TW - 1, xr = (gx + 1) * WPL * TW;  // halo columns
+    auto halo = [&](int y) -> uint32_t {
+        if (lane == 0) return seed_px<DT>(d, y, xl);
+        if (lane == 31) return seed_px<DT>(d, y, xr);
+        return P::MINPX;
+    };
+    // window: marker rows r - 1, r, mask row r, halo pixels
+    uint32_t mu[WPL], mc[WPL], kc[WPL];
+    seed_load<DT, WPL>(d, d.marker, d.pitch_m, y0 - 1, b0, row_bytes, mu);
+    seed_load<DT, WPL>(d, d.marker, d.pitch_m, y0, b0, row_bytes, mc);
+    seed_load<DT, WPL>(d, d.mask, d.pitch_k, y0, b0, row_bytes, kc);
+    uint32_t hu = halo(y0 - 1), hc = halo(y0);
+    // ring slot i holds marker / mask / halo of row r + 1 + i
+    uint32_t rm[kSeedAhead][WPL], rk[kSeedAhead][WPL];
+    uint32_t rh[kSeedAhead];
+#pragma unroll
+    for (int i = 0; i < kSeedAhead; ++i) {
+        const int y = y0 + 1 + i;
+        seed_load<DT, WPL>(d, d.marker, d.pitch_m, y, b0, row_bytes, rm[i]);
+        if (i + 1 < rows) {
+            seed_load<DT, WPL>(d, d.mask, d.pitch_k, y, b0, row_bytes, rk[i]);
+        } else {
+#pragma unroll
+            for (int w = 0; w < WPL; ++w) rk[i][w] = P::MINW;
+        }
+        rh[i] = halo(y);
+    }
+    bool mine = false;
+    for (int r0 = 0; r0 < rows; r0 += kSeedAhead) {
+#pragma unroll
+        for (int i = 0; i < kSeedAhead; ++i) {
+            const int r = r0 + i;
+            if (r >= rows) break;  // warp-uniform
+            uint32_t md[WPL], kn[WPL];
+#pragma unroll
+            for (int w = 0; w < WPL; ++w) {
+                md[w] = rm[i][w];
+                kn[w] = rk[i][w];
+            }
+            const uint32_t hd = rh[i];
+            {
+                const int y = y0 + r + 1 + kSeedAhead;
+                seed_load<DT, WPL>(d, d.marker, d.pitch_m, y, b0, row_bytes, rm[i]);
+                if (r + 1 + kSeedAhead < rows) {
+                    seed_load<DT, WPL>(d, d.mask, d.pitch_k, y, b0, row_bytes, rk[i]);
+                } else {
+#pragma unroll
+                    for (int w = 0; w < WPL; ++w) rk[i][w] = P::MINW;
+                }
+                rh[i] = halo(y);
+            }
+            // what a column offers its side neighbours: itself, or with
+            // 8-connectivity the largest of its three rows
+            uint32_t V[WPL], S[WPL];
+#pragma unroll
+            for (int w = 0; w < WPL; ++w) {
+                V[w] = word_max<DT>(mu[w], md[w]);
+                S[w] = d.conn == 8 ? word_max<DT>(V[w], mc[w]) : mc[w];
+            }
+            const uint32_t hs = d.conn == 8 ? P::mx(P::mx(hu, hc), hd) : hc;
+            uint32_t left = __shfl_up_sync(FULL, S[WPL - 1], 1), right = __shfl_down_sync(FULL, S[0], 1);
+            if (lane == 0) left = BITS == 32 ? hs : hs << (32 - BITS);
+            if (lane == 31) right = hs;
+#pragma unroll
+            for (int w = 0; w < WPL; ++w) {
+                // clamped funnel shifts: a shift of 32 (int32) yields the
+                // adjacent word itself
+                const uint32_t lw = __funnelshift_lc(w == 0 ? left : S[w - 1], S[w], BITS);
+                const uint32_t rw = __funnelshift_rc(S[w], w == WPL - 1 ? right : S[w + 1], BITS);
+                const uint32_t best = word_max<DT>(V[w], word_max<DT>(lw, rw));
+                mine |= word_any_gt<DT>(word_min<DT>(best, kc[w]), mc[w]);
+            }
+#pragma unroll
+            for (int w = 0; w < WPL; ++w) {
+                mu[w] = mc[w];
+                mc[w] = md[w];
+                kc[w] = kn[w];
+            }
+            hu = hc;
+            hc = hd;
+        }
+    }
+    // a tile is bad when one of its lanes saw a pixel to raise
+    const unsigned bad = __ballot_sync(FULL, mine);
+    const int tx = gx * WPL + q;
+    if (lane % LPT == 0 && tx < d.tiles_x) {
+        const bool b = ((bad >> (q * LPT)) & (LPT == 32 ? FULL : ((1u << LPT) - 1u))) != 0u;
+        const unsigned g = (unsigned)d.tile_base + (unsigned)(ty * d.tiles_x + tx);
+        state[g] = b ? (ST_DIRTY | ST_SIDES) : 0u;
+        if (b) list[atomicAdd(nlist, 1u)] = g;
+    }
+}
+
+template <int DT, int WPL>
+__global__ void __launch_bounds__(kSeedThreads, 8)
+    seed_wide_kernel(const ImgDesc d, unsigned* state, unsigned* list, unsigned* nlist) {
+    static_assert(WPL == 2 || WPL == 4, "8- or 16-byte lanes");
+    if (gated_off(d)) return;
     const int gx_n = (d.tiles_x + WPL - 1) / WPL;
     const long long units = (long long)gx_n * d.tiles_y;
     const long long wg = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-    const int TH = d.tile_rows;
-    const long long row_bytes = (long long)d.W * P::BPP;
     for (long long unit = wg; unit < units; unit += nw) {
         const int ty = (int)(unit / gx_n), gx = (int)(unit - (long long)ty * gx_n);
-        const int y0 = ty * TH, rows = min(TH, d.H - y0);
-        const long long b0 = (long long)gx * (128 * WPL) + lane * (4 * WPL);
-        const int xl = gx * WPL * TW - 1, xr = (gx + 1) * WPL * TW;  // halo columns
-        auto halo = [&](int y) -> uint32_t {
-            if (lane == 0) return seed_px<DT>(d, y, xl);
-            if (lane == 31) return seed_px<DT>(d, y, xr);
-            return P::MINPX;
-        };
-        // window: marker rows r - 1, r, mask row r, halo pixels
-        uint32_t mu[WPL], mc[WPL], kc[WPL];
-        seed_load<DT, WPL>(d, d.marker, d.pitch_m, y0 - 1, b0, row_bytes, mu);
-        seed_load<DT, WPL>(d, d.marker, d.pitch_m, y0, b0, row_bytes, mc);
-        seed_load<DT, WPL>(d, d.mask, d.pitch_k, y0, b0, row_bytes, kc);
-        uint32_t hu = halo(y0 - 1), hc = halo(y0);
-        // ring slot i holds marker / mask / halo of row r + 1 + i
-        uint32_t rm[kSeedAhead][WPL], rk[kSeedAhead][WPL];
-        uint32_t rh[kSeedAhead];
-#pragma unroll
-        for (int i = 0; i < kSeedAhead; ++i) {
-            const int y = y0 + 1 + i;
-            seed_load<DT, WPL>(d, d.marker, d.pitch_m, y, b0, row_bytes, rm[i]);
-            if (i + 1 < rows) {
-                seed_load<DT, WPL>(d, d.mask, d.pitch_k, y, b0, row_bytes, rk[i]);
-            } else {
-#pragma unroll
-                for (int w = 0; w < WPL; ++w) rk[i][w] = P::MINW;
-            }
-            rh[i] = halo(y);
+        seed_unit<DT, WPL>(d, ty, gx, state, list, nlist);
+    }
+}
+
+// All images of a job in one launch (their rows on 16-byte boundaries): each
+// CTA forms the prefix of the images' unit counts in shared memory, and a
+// warp finds its unit's image by binary search.  `gate` (nullable) as
+// ImgDesc::gate.
+constexpr int kSeedMaxImages = 1024;
+
+template <int WPL>
+__global__ void __launch_bounds__(kSeedThreads, 6)
+    seed_batch_kernel(const ImgDesc* descs, int nimg, const unsigned* gate, unsigned* state, unsigned* list,
+                      unsigned* nlist) {
+    if (gate != nullptr && *(const volatile unsigned*)gate == 0u) return;
+    __shared__ long long ubase[kSeedMaxImages + 1];
+    __shared__ long long chunk_sum;
+    // the prefix of unit counts, kSeedThreads images at a time
+    if (threadIdx.x == 0) {
+        ubase[0] = 0;
+        chunk_sum = 0;
+    }
+    __syncthreads();
+    for (int i0 = 0; i0 < nimg; i0 += kSeedThreads) {
+        const int i = i0 + (int)threadIdx.x;
+        long long u = 0;
+        if (i < nimg) {
+            const ImgDesc& d = descs[i];
+            u = (long long)((d.tiles_x + WPL - 1) / WPL) * d.tiles_y;
         }
-        bool mine = false;
-        for (int r0 = 0; r0 < rows; r0 += kSeedAhead) {
+        // inclusive scan over the CTA (warp scans, then the warp totals)
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        long long v = u;
 #pragma unroll
-            for (int i = 0; i < kSeedAhead; ++i) {
-                const int r = r0 + i;
-                if (r >= rows) break;  // warp-uniform
-                uint32_t md[WPL], kn[WPL];
-#pragma unroll
-                for (int w = 0; w < WPL; ++w) {
-                    md[w] = rm[i][w];
-                    kn[w] = rk[i][w];
-                }
-                const uint32_t hd = rh[i];
-                {
-                    const int y = y0 + r + 1 + kSeedAhead;
-                    seed_load<DT, WPL>(d, d.marker, d.pitch_m, y, b0, row_bytes, rm[i]);
-                    if (r + 1 + kSeedAhead < rows) {
-                        seed_load<DT, WPL>(d, d.mask, d.pitch_k, y, b0, row_bytes, rk[i]);
-                    } else {
-#pragma unroll
-                        for (int w = 0; w < WPL; ++w) rk[i][w] = P::MINW;
-                    }
-                    rh[i] = halo(y);
-                }
-                // what a column offers its side neighbours: itself, or with
-                // 8-connectivity the largest of its three rows
-                uint32_t V[WPL], S[WPL];
-#pragma unroll
-                for (int w = 0; w < WPL; ++w) {
-                    V[w] = word_max<DT>(mu[w], md[w]);
-                    S[w] = d.conn == 8 ? word_max<DT>(V[w], mc[w]) : mc[w];
-                }
-                const uint32_t hs = d.conn == 8 ? P::mx(P::mx(hu, hc), hd) : hc;
-                uint32_t left = __shfl_up_sync(FULL, S[WPL - 1], 1), right = __shfl_down_sync(FULL, S[0], 1);
-                if (lane == 0) left = BITS == 32 ? hs : hs << (32 - BITS);
-                if (lane == 31) right = hs;
-#pragma unroll
-                for (int w = 0; w < WPL; ++w) {
-                    // clamped funnel shifts: a shift of 32 (int32) yields the
-                    // adjacent word itself
-                    const uint32_t lw = __funnelshift_lc(w == 0 ? left : S[w - 1], S[w], BITS);
-                    const uint32_t rw = __funnelshift_rc(S[w], w == WPL - 1 ? right : S[w + 1], BITS);
-                    const uint32_t best = word_max<DT>(V[w], word_max<DT>(lw, rw));
-                    mine |= word_any_gt<DT>(word_min<DT>(best, kc[w]), mc[w]);
-                }
-#pragma unroll
-                for (int w = 0; w < WPL; ++w) {
-                    mu[w] = mc[w];
-                    mc[w] = md[w];
-                    kc[w] = kn[w];
-                }
-                hu = hc;
-                hc = hd;
-            }
+        for (int dd = 1; dd < 32; dd <<= 1) {
+            const long long t = __shfl_up_sync(FULL, v, dd);
+            if (lane >= dd) v += t;
         }
-        // a tile is bad when one of its lanes saw a pixel to raise
-        const unsigned bad = __ballot_sync(FULL, mine);
-        const int tx = gx * WPL + q;
-        if (lane % LPT == 0 && tx < d.tiles_x) {
-            const bool b = ((bad >> (q * LPT)) & (LPT == 32 ? FULL : ((1u << LPT) - 1u))) != 0u;
-            const unsigned g = (unsigned)d.tile_base + (unsigned)(ty * d.tiles_x + tx);
-            state[g] = b ? (ST_DIRTY | ST_SIDES) : 0u;
-            if (b) list[atomicAdd(nlist, 1u)] = g;
+        __shared__ long long wsum[kSeedThreads / 32];
+        if (lane == 31) wsum[warp] = v;
+        __syncthreads();
+        long long before = chunk_sum;
+        for (int w = 0; w < warp; ++w) before += wsum[w];
+        if (i < nimg) ubase[i + 1] = before + v;
+        __syncthreads();
+        if (threadIdx.x == kSeedThreads - 1) chunk_sum = before + v;
+        __syncthreads();
+    }
+    const long long total = ubase[nimg];
+    const long long wg = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long unit = wg; unit < total; unit += nw) {
+        int lo = 0, hi = nimg - 1;  // the last image whose first unit is <= unit
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (ubase[mid] <= unit)
+                lo = mid;
+            else
+                hi = mid - 1;
         }
+        const ImgDesc d = descs[lo];
+        const long long u = unit - ubase[lo];
+        const int gx_n = (d.tiles_x + WPL - 1) / WPL;
+        const int ty = (int)(u / gx_n), gx = (int)(u - (long long)ty * gx_n);
+        if (d.dtype == DT_U8)
+            seed_unit<DT_U8, WPL>(d, ty, gx, state, list, nlist);
+        else if (d.dtype == DT_U16)
+            seed_unit<DT_U16, WPL>(d, ty, gx, state, list, nlist);
+        else
+            seed_unit<DT_I32, WPL>(d, ty, gx, state, list, nlist);
     }
 }
 
@@ -973,6 +1052,34 @@ cudaError_t launch_top(const ImgDesc& d, void* scratch, unsigned long long* top_
         e = launch_top_t<DT_I32>(a, sms, s);
     if (e == cudaSuccess && launches) *launches += 6;
     return e;
+}
+
+cudaError_t launch_seed_batch(const ImgDesc* dev_descs, const std::vector<ImgDesc>& host_descs, const unsigned* gate,
+                              unsigned* state, unsigned* list, unsigned* nlist, cudaStream_t s, int* launches) {
+    const int nimg = (int)host_descs.size();
+    bool aligned16 = nimg > 0 && nimg <= kSeedMaxImages;
+    long long units = 0;
+    for (const auto& d : host_descs) {
+        aligned16 = aligned16 &&
+                    ((reinterpret_cast<uintptr_t>(d.marker) | reinterpret_cast<uintptr_t>(d.mask)) & 15u) == 0u &&
+                    ((d.pitch_m | d.pitch_k) & 15) == 0;
+        units += (long long)((d.tiles_x + kSeedWords - 1) / kSeedWords) * d.tiles_y;
+    }
+    if (!aligned16) {
+        // one launch per image
+        for (auto d : host_descs) {
+            d.gate = gate;
+            const cudaError_t e = launch_seed(d, state, list, nlist, s, launches);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+    if (units == 0) return cudaSuccess;
+    long long blocks = (units * 32 + kSeedThreads - 1) / kSeedThreads;
+    if (blocks > 152ll * 64) blocks = 152ll * 64;
+    seed_batch_kernel<kSeedWords><<<(unsigned)blocks, kSeedThreads, 0, s>>>(dev_descs, nimg, gate, state, list, nlist);
+    if (launches) ++*launches;
+    return cudaGetLastError();
 }
 
 cudaError_t launch_front_decide(unsigned* gate, unsigned* count, unsigned G, cudaStream_t s, int* launches) {

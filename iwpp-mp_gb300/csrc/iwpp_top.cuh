@@ -3,6 +3,8 @@
 // seeds the tile engine after the whole-image passes.
 #pragma once
 
+#include <vector>
+
 #include "iwpp_device.cuh"
 
 namespace iwpp {
@@ -21,6 +23,13 @@ cudaError_t launch_top(const ImgDesc& d, void* scratch, unsigned long long* top_
 // while *d.gate is 0 (so do the top-level stage and the sweeps).
 cudaError_t launch_seed(const ImgDesc& d, unsigned* state, unsigned* list, unsigned* nlist, cudaStream_t s,
                         int* launches);
+// The same check over every image of a job in one launch when their rows
+// start on 16-byte boundaries (and the job has at most 1024 images), else
+// one launch per image.  `dev_descs`: the job's descriptors in device
+// memory (`host_descs` the same on the host); `gate` (nullable) as
+// ImgDesc::gate.
+cudaError_t launch_seed_batch(const ImgDesc* dev_descs, const std::vector<ImgDesc>& host_descs, const unsigned* gate,
+                              unsigned* state, unsigned* list, unsigned* nlist, cudaStream_t s, int* launches);
 // After a seed check over a job's G tiles (its count in *count): *gate = 1
 // and *count = 0 when the initial front is small enough for the front stage
 // to pay, else *gate = 0 (the list stands and seeds the engine).
