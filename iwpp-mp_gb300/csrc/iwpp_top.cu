@@ -612,22 +612,14 @@ __global__ void __launch_bounds__(kTopThreads, 4) top_apply_label_kernel(TopArgs
 }
 
 // --------------------------------------------------------- engine seeding
-// After the front stage and the whole-image passes the tile engine must
-// still visit every tile holding a pixel that a neighbour could raise (with
-// 8-connectivity: across the diagonals too).  One warp per engine tile (TH
-// rows, 128 bytes wide) streams the tile's rows with the rows above and
-// below, one word per lane, neighbours across lanes by shuffles and across
-// tiles by the halo columns (lanes 0 / 31); it marks a tile with such a
+// After the front stage and the whole-image passes (or instead of them) the
+// tile engine must visit every tile holding a pixel that a neighbour could
+// raise (with 8-connectivity: across the diagonals too).  The check streams
+// each tile's rows with the rows above and below, marks a tile with such a
 // pixel DIRTY on all sides and appends it to the seed list; other tiles get
 // state 0.
-template <int DT>
-__device__ __forceinline__ uint32_t seed_word(const ImgDesc& d, const unsigned char* base, long long pitch, int y,
-                                              int px0) {
-    using P = Px<DT>;
-    if (y < 0 || y >= d.H || px0 >= d.W) return P::MINW;
-    return load_word_plain<DT>(base + (size_t)y * pitch + (size_t)px0 * P::BPP, d.W - px0, false);
-}
 
+// A marker pixel, the least value outside the image.
 template <int DT>
 __device__ __forceinline__ uint32_t seed_px(const ImgDesc& d, int y, int x) {
     using P = Px<DT>;
@@ -635,86 +627,14 @@ __device__ __forceinline__ uint32_t seed_px(const ImgDesc& d, int y, int x) {
     return P::ld_px(d.marker + (size_t)y * d.pitch_m + (size_t)x * P::BPP);
 }
 
-template <int DT>
-__global__ void seed_kernel(const ImgDesc d, unsigned* state, unsigned* list, unsigned* nlist) {
-    if (gated_off(d)) return;
-    using P = Px<DT>;
-    constexpr int N = P::PPW;
-    constexpr int TW = 32 * N;
-    const int lane = threadIdx.x & 31;
-    const long long tiles = (long long)d.tiles_x * d.tiles_y;
-    const long long wg = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-    const int TH = d.tile_rows;
-    for (long long t = wg; t < tiles; t += nw) {
-        const int ty = (int)(t / d.tiles_x), tx = (int)(t - (long long)ty * d.tiles_x);
-        const int x0 = tx * TW, y0 = ty * TH, rows = min(TH, d.H - y0);
-        const int px0 = x0 + lane * N;
-        // marker words of rows y - 1, y, y + 1 (rolling), and for lanes 0 / 31
-        // the halo column pixel beside the tile in the same three rows
-        uint32_t wu = seed_word<DT>(d, d.marker, d.pitch_m, y0 - 1, px0);
-        uint32_t wc = seed_word<DT>(d, d.marker, d.pitch_m, y0, px0);
-        const int hx = lane == 0 ? x0 - 1 : x0 + TW;
-        uint32_t hu = seed_px<DT>(d, y0 - 1, hx), hc = seed_px<DT>(d, y0, hx);
-        bool bad = false;
-        for (int r = 0; r < rows; ++r) {
-            const int y = y0 + r;
-            const uint32_t wd = seed_word<DT>(d, d.marker, d.pitch_m, y + 1, px0);
-            const uint32_t wk = seed_word<DT>(d, d.mask, d.pitch_k, y, px0);
-            const uint32_t hd = seed_px<DT>(d, y + 1, hx);
-            uint32_t u[N], c[N], dn[N], k[N];
-            P::unpack(wu, u);
-            P::unpack(wc, c);
-            P::unpack(wd, dn);
-            P::unpack(wk, k);
-            // per column: the larger of the pixels above and below (the
-            // vertical neighbours) and the largest of all three (what a
-            // column offers its side neighbours with 8-connectivity)
-            uint32_t v2[N], v3[N];
-#pragma unroll
-            for (int j = 0; j < N; ++j) {
-                v2[j] = P::mx(u[j], dn[j]);
-                v3[j] = P::mx(v2[j], c[j]);
-            }
-            // the columns left of the lane's first pixel and right of its last
-            const uint32_t side_l = d.conn == 8 ? v3[N - 1] : c[N - 1];
-            const uint32_t side_r = d.conn == 8 ? v3[0] : c[0];
-            uint32_t left = __shfl_up_sync(FULL, side_l, 1), right = __shfl_down_sync(FULL, side_r, 1);
-            const uint32_t halo = d.conn == 8 ? P::mx(P::mx(hu, hc), hd) : hc;
-            if (lane == 0) left = halo;
-            if (lane == 31) right = halo;
-            bool mine = false;
-#pragma unroll
-            for (int j = 0; j < N; ++j) {
-                const uint32_t l = j == 0 ? left : (d.conn == 8 ? v3[j - 1] : c[j - 1]);
-                const uint32_t rr = j == N - 1 ? right : (d.conn == 8 ? v3[j + 1] : c[j + 1]);
-                const uint32_t best = P::mx(v2[j], P::mx(l, rr));
-                mine |= P::gt(P::mn(best, k[j]), c[j]) && px0 + j < d.W;
-            }
-            if (__any_sync(FULL, mine)) {
-                bad = true;
-                break;
-            }
-            wu = wc;
-            wc = wd;
-            hu = hc;
-            hc = hd;
-        }
-        const unsigned g = (unsigned)d.tile_base + (unsigned)t;
-        if (lane == 0) {
-            state[g] = bad ? (ST_DIRTY | ST_SIDES) : 0u;
-            if (bad) list[atomicAdd(nlist, 1u)] = g;
-        }
-    }
-}
-
-// The same check with wide lanes: a lane holds WPL words (8 or 16 bytes) of
+// The check with wide lanes: a lane holds WPL words (8 or 16 bytes) of
 // a row, so a warp covers WPL engine tiles side by side (32 / WPL lanes
 // each); the words are updated with byte / half-word SIMD, the side
 // neighbours of a word's pixels come from funnel shifts of the adjacent
-// words, and rows are loaded kSeedAhead ahead into a register ring.  Rows
-// must start on 16-byte boundaries (both planes).  Eight-byte lanes keep
-// the registers per thread low enough for eight CTAs per SM.
+// words, and rows are loaded kSeedAhead ahead into a register ring (one
+// vector load per lane where the address allows it, else word by word;
+// rows start on 4-byte boundaries).  Eight-byte lanes keep the registers
+// per thread low enough for eight CTAs per SM.
 constexpr int kSeedAhead = 2;
 constexpr int kSeedThreads = 128;
 constexpr int kSeedWords = 2;  // words per lane
@@ -729,7 +649,7 @@ __device__ __forceinline__ void seed_load(const ImgDesc& d, const unsigned char*
     for (int i = 0; i < WPL; ++i) w[i] = P::MINW;
     if (y < 0 || y >= d.H || b0 >= row_bytes) return;
     const unsigned char* p = base + (size_t)y * pitch + b0;
-    if (b0 + 4 * WPL <= row_bytes) {
+    if (b0 + 4 * WPL <= row_bytes && (reinterpret_cast<uintptr_t>(p) & (4 * WPL - 1)) == 0) {
         if constexpr (WPL == 4) {
             const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
             w[0] = v.x;
@@ -743,6 +663,7 @@ __device__ __forceinline__ void seed_load(const ImgDesc& d, const unsigned char*
         }
         return;
     }
+    // rows only 4-byte aligned, or the row's last lane: word by word
 #pragma unroll
     for (int i = 0; i < WPL; ++i) {
         const long long b = b0 + 4 * i;
@@ -1057,15 +978,9 @@ cudaError_t launch_top(const ImgDesc& d, void* scratch, unsigned long long* top_
 cudaError_t launch_seed_batch(const ImgDesc* dev_descs, const std::vector<ImgDesc>& host_descs, const unsigned* gate,
                               unsigned* state, unsigned* list, unsigned* nlist, cudaStream_t s, int* launches) {
     const int nimg = (int)host_descs.size();
-    bool aligned16 = nimg > 0 && nimg <= kSeedMaxImages;
     long long units = 0;
-    for (const auto& d : host_descs) {
-        aligned16 = aligned16 &&
-                    ((reinterpret_cast<uintptr_t>(d.marker) | reinterpret_cast<uintptr_t>(d.mask)) & 15u) == 0u &&
-                    ((d.pitch_m | d.pitch_k) & 15) == 0;
-        units += (long long)((d.tiles_x + kSeedWords - 1) / kSeedWords) * d.tiles_y;
-    }
-    if (!aligned16) {
+    for (const auto& d : host_descs) units += (long long)((d.tiles_x + kSeedWords - 1) / kSeedWords) * d.tiles_y;
+    if (nimg == 0 || nimg > kSeedMaxImages) {
         // one launch per image
         for (auto d : host_descs) {
             d.gate = gate;
@@ -1091,34 +1006,17 @@ cudaError_t launch_front_decide(unsigned* gate, unsigned* count, unsigned G, cud
 cudaError_t launch_seed(const ImgDesc& d, unsigned* state, unsigned* list, unsigned* nlist, cudaStream_t s,
                         int* launches) {
     if (d.W == 0 || d.H == 0) return cudaSuccess;
-    const bool aligned16 =
-        ((reinterpret_cast<uintptr_t>(d.marker) | reinterpret_cast<uintptr_t>(d.mask)) & 15u) == 0u &&
-        ((d.pitch_m | d.pitch_k) & 15) == 0;
-    if (aligned16) {
-        constexpr int WPL = kSeedWords;
-        const long long units = (long long)((d.tiles_x + WPL - 1) / WPL) * d.tiles_y;
-        long long blocks = (units * 32 + kSeedThreads - 1) / kSeedThreads;
-        if (blocks > 152ll * 64) blocks = 152ll * 64;
-        if (blocks < 1) blocks = 1;
-        if (d.dtype == DT_U8)
-            seed_wide_kernel<DT_U8, WPL><<<(unsigned)blocks, kSeedThreads, 0, s>>>(d, state, list, nlist);
-        else if (d.dtype == DT_U16)
-            seed_wide_kernel<DT_U16, WPL><<<(unsigned)blocks, kSeedThreads, 0, s>>>(d, state, list, nlist);
-        else
-            seed_wide_kernel<DT_I32, WPL><<<(unsigned)blocks, kSeedThreads, 0, s>>>(d, state, list, nlist);
-        if (launches) ++*launches;
-        return cudaGetLastError();
-    }
-    const long long tiles = (long long)d.tiles_x * d.tiles_y;
-    long long blocks = (tiles * 32 + 255) / 256;
-    if (blocks > 152ll * 16) blocks = 152ll * 16;
+    constexpr int WPL = kSeedWords;
+    const long long units = (long long)((d.tiles_x + WPL - 1) / WPL) * d.tiles_y;
+    long long blocks = (units * 32 + kSeedThreads - 1) / kSeedThreads;
+    if (blocks > 152ll * 64) blocks = 152ll * 64;
     if (blocks < 1) blocks = 1;
     if (d.dtype == DT_U8)
-        seed_kernel<DT_U8><<<(unsigned)blocks, 256, 0, s>>>(d, state, list, nlist);
+        seed_wide_kernel<DT_U8, WPL><<<(unsigned)blocks, kSeedThreads, 0, s>>>(d, state, list, nlist);
     else if (d.dtype == DT_U16)
-        seed_kernel<DT_U16><<<(unsigned)blocks, 256, 0, s>>>(d, state, list, nlist);
+        seed_wide_kernel<DT_U16, WPL><<<(unsigned)blocks, kSeedThreads, 0, s>>>(d, state, list, nlist);
     else
-        seed_kernel<DT_I32><<<(unsigned)blocks, 256, 0, s>>>(d, state, list, nlist);
+        seed_wide_kernel<DT_I32, WPL><<<(unsigned)blocks, kSeedThreads, 0, s>>>(d, state, list, nlist);
     if (launches) ++*launches;
     return cudaGetLastError();
 }

@@ -23,9 +23,8 @@ cudaError_t launch_top(const ImgDesc& d, void* scratch, unsigned long long* top_
 // while *d.gate is 0 (so do the top-level stage and the sweeps).
 cudaError_t launch_seed(const ImgDesc& d, unsigned* state, unsigned* list, unsigned* nlist, cudaStream_t s,
                         int* launches);
-// The same check over every image of a job in one launch when their rows
-// start on 16-byte boundaries (and the job has at most 1024 images), else
-// one launch per image.  `dev_descs`: the job's descriptors in device
+// The same check over every image of a job in one launch (one launch per
+// image when the job has more than 1024).  `dev_descs`: the job's descriptors in device
 // memory (`host_descs` the same on the host); `gate` (nullable) as
 // ImgDesc::gate.
 cudaError_t launch_seed_batch(const ImgDesc* dev_descs, const std::vector<ImgDesc>& host_descs, const unsigned* gate,
