@@ -191,6 +191,17 @@ def timed_oracle(marker, mask, conn):
     return res, time.perf_counter() - t0
 
 
+def inputs_sha256(*arrays):
+    """sha256 over the bytes of the generated input arrays, in order (the
+    record of which synthetic inputs a result was measured on)."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(a.tobytes())
+    return h.hexdigest()
+
+
 def traffic_from_profile(key):
     """DRAM bytes per launch recorded from an ncu capture (profiles/)."""
     path = os.path.join(REPO, "profiles", "dram_traffic.json")
@@ -329,6 +340,7 @@ def bench_batched(args, dev, variant):
     t_plan = statistics.median(graph[max(args.warmup, 3):])
     return {"workload": f"64 images, sizes log-uniform 512..4096 x 512..3072 (seed 3, {px / 1e6:.1f} Mpx), "
                         "uint8/uint16, 4/8-conn, h-dome h in [5,120]; device-resident",
+            "inputs_sha256": inputs_sha256(*[a for pair in imgs for a in pair]),
             "plan_gpx_s": px / t_plan / 1e9, "sequential_gpx_s": px / t_seq / 1e9, "speedup": t_seq / t_plan,
             "plan_ms": t_plan * 1e3, "sequential_ms": t_seq * 1e3,
             "plan_hbm_frac": nbytes / t_plan / 1e9 / peak_hbm()[0], "tiles": st.tiles, "visits": st.visits,
@@ -443,6 +455,7 @@ def bench_served(args, dev, variant):
                         f"({px / n_req / 1e6:.2f} Mpx mean), uint8 80% / uint16 20%, 8-conn, "
                         "h-dome or 0.01% sparse seeds; pinned host buffers, H2D + D2H included",
             "offered_gpx_s": px / times[-1] / 1e9, "lanes": args.lanes, "distinct_images": len(set(which)),
+            "inputs_sha256": inputs_sha256(*[a for pair in imgs for a in pair]),
             "open_loop": served, "closed_loop": saturated,
             "plain_per_request_gpx_s": px / t_plain / 1e9, "plain_bitexact": plain_ok,
             "speedup_vs_plain": saturated["gpx_s"] / (px / t_plain / 1e9),
@@ -557,6 +570,7 @@ def bench_config1(args, dev, variant, handle):
     secs = time.perf_counter() - ts
     e2e_ok = all(np.array_equal(host_out[i].numpy(), results[i]) for i in range(len(cases)))
     return {"workload": CONFIG1, "variant": variant, "steps": steps, "gpx_s": px_step * steps / (elapsed / 1e3) / 1e9,
+            "inputs_sha256": inputs_sha256(mask_np, *[m for _, _, m in cases]),
             "ms_per_step": elapsed / steps, "mean_reconstruction_ms": mean_ms,
             "hbm_frac": 3 * W * H / (mean_ms / 1e3) / 1e9 / peak, "bitexact_vs_oracle": bitexact,
             "dram_bytes_per_reconstruction": traffic_from_profile("config1"),
@@ -599,7 +613,7 @@ def bench_spiral_types(args, dev, variant, handle):
         t = statistics.median(times) / 1e3
         res[name] = {"ms": t * 1e3, "gpx_s": W * H / t / 1e9, "hbm_frac": 3 * W * H * bpp / t / 1e9 / peak,
                      "visits": st.visits, "tiles": st.tiles, "top_pixels": st.top_pixels,
-                     "untuned_ms": st0.device_ms,
+                     "untuned_ms": st0.device_ms, "inputs_sha256": inputs_sha256(marker, mask),
                      "autotuned": {k_: tuned[k_] for k_ in ("tile_rows", "solver", "init_passes", "front_passes")}}
         pending.append((name, fut, _from_dev(m, marker.dtype)))
         del m, m0, k
@@ -805,6 +819,7 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "variant": variant,
                    "autotuned": {k_: tuned[k_] for k_ in ("tile_rows", "solver", "init_passes", "front_passes")},
                    "l2": "inputs larger than L2: working + pristine marker + mask = 805 MB per step",
+                   "inputs_sha256": {"marker": inputs_sha256(marker_np), "mask": inputs_sha256(mask_np)},
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "bitexact": bitexact, "bitexact_timed_steps": timed_ok, "fixed_point": fixed_point_ok,
         "untuned_ms": st_untuned.device_ms,
