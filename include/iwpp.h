@@ -198,10 +198,12 @@ IWPP_API int iwpp_queue_selftest(int device, int variant, int grid_side, int cop
 /* No counterpart in the reference (its tile size, queue sizes and number of
  * initial passes are compile-time constants, IWPP MP/include/
  * MorphologicalReconstruction.cuh:6-7, and commented-out sweeps, MR.cu:792-795).
- * Times candidate configurations on the caller's own batch -- tile rows
- * 64 / 32 x in-tile solver, then front passes on, then (if they lost) 1, 2,
- * 4, ... 64 initial raster + anti-raster passes while each doubling is
- * faster, then (mutex / double queues) queue capacity 1x / 16x the tiles --
+ * Times candidate configurations on the caller's own batch -- the untuned
+ * default for large images, tile rows 64 / 32 x in-tile solver, the best of
+ * those started from a seed check, the front stage with 1 / 2 / 3 / 4 / 8
+ * whole-image passes, then (if it lost) 1, 2, 4, ... 64 initial raster +
+ * anti-raster passes while each doubling is faster, then (mutex / double
+ * queues) queue capacity 1x / 16x the tiles --
  * each the median of `repeats` runs (0 = 3) from the same markers, records
  * the fastest in the process-wide tuning table under the batch's workload
  * class (queue variant, pixel type, connectivity, floor(log2(pixels)),

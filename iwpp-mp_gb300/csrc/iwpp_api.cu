@@ -206,8 +206,9 @@ struct Layout {
     size_t off_imgs, off_tmaps, off_state, off_q0, off_q1, off_sweep, off_list, total;
 };
 
-// sweep_bytes: scratch of the whole-image sweeps or front passes run before
-// the engine; seed_list: room for the engine's seed list after front passes
+// sweep_bytes: scratch of the whole-image sweeps or the front stage run
+// before the engine; seed_list: room for the engine's seed list after a seed
+// check
 // (G ids and their count)
 Layout layout_for(long long n_imgs, long long G, long long cap, bool two_queues, size_t sweep_bytes = 0,
                   bool seed_list = false) {
@@ -344,7 +345,7 @@ int build_job(Job& job, const iwpp_image* imgs, int n, int variant, const iwpp_c
             if (job.cfg.dflt_solver) job.cfg.solver = e.solver;
             if (job.cfg.dflt_init) {
                 job.cfg.init_passes = e.init_passes;
-                job.cfg.dflt_init = false;  // the table's count stands, also with front passes
+                job.cfg.dflt_init = false;  // the table's count stands, also with the front stage
             }
             if (job.cfg.dflt_queue && e.queue_mult > 0) job.cfg.queue_capacity = -(long long)e.queue_mult;
             if (job.cfg.dflt_front) job.cfg.front_passes = tune_front_code(e.front_passes);

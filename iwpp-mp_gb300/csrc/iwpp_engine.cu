@@ -12,7 +12,7 @@ __device__ __forceinline__ int ld_volatile(const int* p) { return *(const volati
 __device__ __forceinline__ void set_error(Ctrl* c, unsigned code) { atomicCAS(&c->error, 0u, code); }
 
 // Async ring: positions below this are the job's initial entries (every
-// tile, or the seed list after front passes), the rest map to ring slots.
+// tile, or the seed list after the front stage), the rest map to ring slots.
 __device__ __forceinline__ unsigned ring_base(const EngineArgs& a) {
     return a.init_list ? ld_volatile(&a.ctrl->ninit) : a.G;
 }
@@ -641,7 +641,7 @@ __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
 
 // ------------------------------------------------------- async worker
 // Ring positions 0..n0-1 are the initial tiles (no storage: every tile in
-// id order, or the seed list after front passes); position p >= n0 lives in
+// id order, or the seed list after the front stage); position p >= n0 lives in
 // slot (p - n0) % cap.  A warp claims the next position with one
 // atomicAdd and waits for a producer to fill it.  Every filled position is
 // claimed by exactly one warp, and when `pending` (filled, unfinished
@@ -876,7 +876,7 @@ __global__ void engine_init_kernel(EngineArgs a, int variant) {
         c->rounds = 0u;
         c->bar_count = 0u;
         c->bar_gen = 0u;
-        if (!a.front) c->error = 0u;  // else the front passes' error stands
+        if (!a.front) c->error = 0u;  // else the seed check's job keeps its error word
         c->lock_next = 0u;
         c->lock_word = (unsigned long long)(n0 < a.cap ? n0 : a.cap) << 32;  // ticket 0 served
         c->pending = (int)(n0 < a.cap ? n0 : a.cap);

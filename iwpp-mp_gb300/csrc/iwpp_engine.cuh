@@ -68,7 +68,7 @@ struct Ctrl {
     unsigned long long row_steps;
     unsigned long long phase[5];  // cycles: queue read, fetch, processing, dump, queue write
     unsigned long long top_pixels;    // pixels the top-level stage labelled
-    unsigned ninit;     // initial entries (every tile, or the seed list after front passes)
+    unsigned ninit;     // initial entries (every tile, or the seed list after the front stage)
     unsigned front_gate;  // front stage decided on the device: 1 run it, 0 leave the job to the engine
     unsigned idle;        // mutex: warps waiting for work
 };
@@ -91,7 +91,7 @@ struct EngineArgs {
                       // clean tiles are released at once
     int front_ran;    // the front stage ran (not gated)
     int front_gated;  // the device decided whether the stage ran (Ctrl::front_gate)
-    // After front passes: the tiles to start from (ids) and their count (a
+    // After the front stage: the tiles to start from (ids) and their count (a
     // device counter); nullptr: every tile, in id order.  The tile states
     // were set by the seed check.
     const unsigned* init_list;

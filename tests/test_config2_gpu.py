@@ -3,8 +3,9 @@ a one-pixel corridor of 1 048 194 pixels at the dtype maximum, threaded
 through smoothed noise, seeded at its start) in uint8, uint16 and int32,
 8-connectivity, at full size: the GPU result must equal the CPU oracle bit
 for bit under every schedule the library offers for them -- the untuned
-default, the fixed whole-image passes, and the front passes restricted to
-changed tiles.  The oracle runs on host threads while the GPU works.
+default, the fixed whole-image passes, and the front stage (top-level
+labelling, passes, the engine from a seed check).  The oracle runs on host
+threads while the GPU works.
 
 int32 masks span the full signed range, so negative values next to the
 image border exercise the "outside pixels do not exist" rule of the
