@@ -727,18 +727,22 @@ int enqueue_job(const Job& job, Workspace& ws, cudaStream_t s, int device, bool 
                                   seed_count, s, &nl);
         if (e != cudaSuccess) return cuda_status(e);
     }
-    e = engine_launch_init(a, job.variant, s);
-    if (e != cudaSuccess) return cuda_status(e);
-    ++nl;
+    long long grid = 1;
     if (job.G > 0) {
         LaunchInfo li;
         e = engine_prepare(job.variant, job.tile_rows, device, &li);
         if (e != cudaSuccess) return cuda_status(e);
-        long long grid = li.grid;
+        grid = li.grid;
         const long long useful = (job.G + kWarps - 1) / kWarps;
         if (grid > useful) grid = useful;
         if (job.cfg.grid_ctas > 0 && job.cfg.grid_ctas < grid) grid = job.cfg.grid_ctas;
         if (grid < 1) grid = 1;
+    }
+    a.grid = (int)grid;
+    e = engine_launch_init(a, job.variant, s);
+    if (e != cudaSuccess) return cuda_status(e);
+    ++nl;
+    if (job.G > 0) {
         e = engine_launch(a, job.variant, job.tile_rows, (int)grid, s);
         if (e != cudaSuccess) return cuda_status(e);
         ++nl;

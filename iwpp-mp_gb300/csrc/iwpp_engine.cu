@@ -550,6 +550,17 @@ __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
         s_cq.waiting = 0;
     }
     __syncthreads();
+    // this CTA's slice of the initial stack, without the lock (it lies above
+    // the stack's top, and `pending` counts it already); the lowest position
+    // ends on the buffer's top, so it is taken first, as from the stack
+    {
+        const unsigned pf = ld_volatile(&a.ctrl->prefill);
+        const unsigned base = ld_volatile(&a.ctrl->prefill_base) + blockIdx.x * pf;
+        for (unsigned j = threadIdx.x; j < pf; j += blockDim.x)
+            s_cq.e[j] = __ldcg(&a.q0[base + pf - 1u - j]);
+        if (threadIdx.x == 0) s_cq.n = (int)pf;
+        __syncthreads();
+    }
     long long idle_since = 0;
     unsigned idle_progress = 0u;
     unsigned ns = 64;
@@ -878,7 +889,16 @@ __global__ void engine_init_kernel(EngineArgs a, int variant) {
         c->bar_gen = 0u;
         if (!a.front) c->error = 0u;  // else the seed check's job keeps its error word
         c->lock_next = 0u;
-        c->lock_word = (unsigned long long)(n0 < a.cap ? n0 : a.cap) << 32;  // ticket 0 served
+        // the mutex stack's first entries: a slice per CTA taken without the
+        // lock when the kernel starts (at most half a CTA buffer each), the
+        // rest stacked
+        const unsigned stacked = n0 < a.cap ? n0 : a.cap;
+        const unsigned ctas = a.grid > 0 ? (unsigned)a.grid : 1u;
+        unsigned pf = variant == VAR_MUTEX ? stacked / ctas : 0u;
+        if (pf > (unsigned)kMutexPrefill) pf = (unsigned)kMutexPrefill;
+        c->prefill = pf;
+        c->prefill_base = stacked - pf * ctas;
+        c->lock_word = (unsigned long long)(stacked - pf * ctas) << 32;  // ticket 0 served
         c->pending = (int)(n0 < a.cap ? n0 : a.cap);
         c->progress = 0u;
         c->idle = 0u;

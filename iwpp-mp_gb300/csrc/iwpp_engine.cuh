@@ -39,6 +39,7 @@ enum : unsigned { DEV_OK = 0u, DEV_ERR_TIMEOUT = 3u, DEV_ERR_OVERFLOW = 5u, DEV_
 
 constexpr int kWarps = 4;       // warps (independent tile workers) per CTA
 constexpr int kMutexBatch = 8;  // entries taken per mutex acquisition
+constexpr int kMutexPrefill = 32;  // initial stack entries a CTA takes without the lock
 
 struct Ctrl {
     unsigned rn;        // entries in the read queue (this round)
@@ -71,6 +72,8 @@ struct Ctrl {
     unsigned ninit;     // initial entries (every tile, or the seed list after the front stage)
     unsigned front_gate;  // front stage decided on the device: 1 run it, 0 leave the job to the engine
     unsigned idle;        // mutex: warps waiting for work
+    unsigned prefill;     // mutex: initial entries each CTA takes without the lock
+    unsigned prefill_base;  // mutex: stack position of CTA 0's slice (the stack's top below it)
 };
 
 struct EngineArgs {
@@ -86,6 +89,7 @@ struct EngineArgs {
     int max_restarts;
     int solver;  // 0 automatic, 1 row sweeps, 2 passes
     int phantom;  // test hook: one unit of work that never arrives (every wait runs out)
+    int grid;     // CTAs of the engine launch (the mutex stack's first entries are split among them)
     int front;    // a seed check ran: the job's error word and top-pixel count stand
     int states_set;   // the seed check set every tile's state: the queue holds every tile in order,
                       // clean tiles are released at once
