@@ -30,7 +30,10 @@ configuration fields, which the tuning table fills.
 
 Sub-results in the same line (skipped with --no-extras):
   config1 : the six 4096^2 uint8 reconstructions (connectivity {4, 8} x
-          h-dome h {10, 40, 100}), device-resident and end to end.
+          h-dome h {10, 40, 100}), device-resident and end to end, after
+          the autotuner has seen each connectivity's image class once
+          (--config1-only: the untuned default, or --config1-solver's
+          solver, the profiled launches).
   batched : 64 uneven images in one CUDA-graph plan vs 64 sequential plain
           calls, Gpixels/s of each, bit-exact against each other and the
           oracle.
@@ -507,10 +510,12 @@ def bench_served(args, dev, variant):
             "bitexact_vs_oracle": oracle_ok}
 
 
-def bench_config1(args, dev, variant, handle):
+def bench_config1(args, dev, variant, handle, tune=True):
     """The six 4096^2 uint8 reconstructions of configuration 1 per step:
     device-resident (events on the launching stream) and end to end from
-    pinned host buffers, each image through the per-image C-ABI call."""
+    pinned host buffers, each image through the per-image C-ABI call with
+    the default configuration, after the autotuner has seen each
+    connectivity's image class once."""
     import numpy as np
     import torch
 
@@ -527,6 +532,20 @@ def bench_config1(args, dev, variant, handle):
     conns = [c for c, _, _ in cases]
     stream = torch.cuda.Stream(dev)
     steps = max(args.steps, 20)
+    solver = getattr(args, "config1_solver", None)
+    cfg = None if solver is None else __import__("ctypes").byref(iwpp.Config.make(solver=solver))
+
+    # the autotuner once per image class (4096^2 uint8 at each connectivity,
+    # tuned on its h = 40 image); the default calls below read its table
+    tuned = {}
+    for conn in sorted(set(conns)) if tune else ():
+        i = next(j for j, (c, h, _) in enumerate(cases) if c == conn and h == 40)
+        probe = pristine[i].clone()
+        with torch.cuda.stream(stream):
+            t = iwpp.autotune([(probe, mask, conn)], variant=variant, handle=handle, stream=stream)
+        tuned[f"conn{conn}"] = {k_: t[k_] for k_ in ("tile_rows", "solver", "init_passes", "front_passes")}
+        del probe
+    torch.cuda.synchronize()
 
     def step(ev_pairs=None):
         for i in range(len(cases)):
@@ -534,7 +553,7 @@ def bench_config1(args, dev, variant, handle):
             if ev_pairs is not None:
                 ev_pairs[i][0].record(stream)
             st = lib.iwpp_reconstruct_async(handle.ptr, work[i].data_ptr(), mask.data_ptr(), W, W, W, H, 0, conns[i],
-                                            vcode, None, stream.cuda_stream)
+                                            vcode, cfg, stream.cuda_stream)
             if st != 0:
                 raise iwpp.IwppError(st, "iwpp_reconstruct_async")
             if ev_pairs is not None:
@@ -591,7 +610,7 @@ def bench_config1(args, dev, variant, handle):
                 ev_in[b].record(s_in)
             s_run.wait_event(ev_in[b])
             st = lib.iwpp_reconstruct_async(handle.ptr, dmb[b].data_ptr(), dkb[b].data_ptr(), W, W, W, H, 0,
-                                            conns[i], vcode, None, s_run.cuda_stream)
+                                            conns[i], vcode, cfg, s_run.cuda_stream)
             if st != 0:
                 raise iwpp.IwppError(st, "iwpp_reconstruct_async")
             ev_run[b].record(s_run)
@@ -614,7 +633,8 @@ def bench_config1(args, dev, variant, handle):
         pipelined_step(finish=k == e2e_steps - 1)
     secs = time.perf_counter() - ts
     e2e_ok = all(np.array_equal(host_out[i].numpy(), results[i]) for i in range(len(cases)))
-    return {"workload": CONFIG1, "variant": variant, "steps": steps, "gpx_s": px_step * steps / (elapsed / 1e3) / 1e9,
+    return {"workload": CONFIG1, "variant": variant, "autotuned": tuned or None, "solver": solver, "steps": steps,
+            "gpx_s": px_step * steps / (elapsed / 1e3) / 1e9,
             "inputs_sha256": inputs_sha256(mask_np, *[m for _, _, m in cases]),
             "ms_per_step": elapsed / steps, "mean_reconstruction_ms": mean_ms,
             "hbm_frac": 3 * W * H / (mean_ms / 1e3) / 1e9 / peak, "bitexact_vs_oracle": bitexact,
@@ -922,6 +942,9 @@ def main():
     ap.add_argument("--spiral-reps", type=int, default=3)
     ap.add_argument("--config1-only", action="store_true",
                     help="only the six 4096^2 configuration-1 reconstructions with --variant (one JSON line)")
+    ap.add_argument("--config1-solver", type=int, default=None, choices=[0, 1, 2, 3],
+                    help="with --config1-only: every call with this in-tile solver (the configuration the "
+                         "autotuner picks, without its launches before the profiled ones)")
     ap.add_argument("--profile-headline", type=int, default=0, metavar="N",
                     help="only N reconstructions of the headline image with the front stage (for profilers)")
     ap.add_argument("--profile-passes", type=int, default=2,
@@ -975,7 +998,7 @@ def run_config1_only(args):
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     handle = iwpp.Handle(0)
-    res = bench_config1(args, dev, args.variant, handle)
+    res = bench_config1(args, dev, args.variant, handle, tune=False)
     handle.close()
     print(json.dumps({"config1": res}), flush=True)
     return 0

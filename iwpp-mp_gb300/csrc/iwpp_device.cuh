@@ -459,6 +459,53 @@ __device__ __forceinline__ unsigned long long vpass(WarpSmem<TH>& sm, int lane, 
         __syncwarp();
         return warp_or64(chg);
     }
+    if (CONN == 8 && DT != DT_I32) {
+        // packed 8-connected rows: the previous row's three-pixel maximum
+        // from the word itself and the words 16 bits to either side, built
+        // by funnel shifts from the neighbour lanes' words (the tile's halo
+        // columns at lanes 0 / 31).  uint16 words are u16x2 as they are;
+        // uint8 words run as their even (lo) and odd (hi) bytes, where the
+        // even bytes' neighbours are the odd half and the odd half shifted
+        // in from the left, the odd bytes' the even half and the even half
+        // shifted in from the right.
+        constexpr uint32_t E = 0x00ff00ffu;
+        const uint32_t first_prev = sm.tm[(DOWN ? first - 1 : first + 1) * 32 + lane];
+        uint32_t plo = DT == DT_U8 ? first_prev & E : first_prev;
+        uint32_t phi = (first_prev >> 8) & E;
+#pragma unroll 4
+        for (int i = 0; i < count; ++i) {
+            const int r = DOWN ? first + i : first - i;
+            const int rp = DOWN ? r - 1 : r + 1;
+            const uint32_t old = sm.tm[r * 32 + lane];
+            const uint32_t kw = sm.tk[r * 32 + lane];
+            uint32_t nw;
+            if (DT == DT_U8) {
+                uint32_t left = __shfl_up_sync(FULL, phi, 1), right = __shfl_down_sync(FULL, plo, 1);
+                if (lane == 0) left = sm.hLm[rp] << 16;
+                if (lane == 31) right = sm.hRm[rp];
+                const uint32_t dlo = __vimax3_u16x2(plo, phi, __funnelshift_l(left, phi, 16));
+                const uint32_t dhi = __vimax3_u16x2(phi, plo, __funnelshift_r(plo, right, 16));
+                plo = __vmaxu2(old & E, __vminu2(dlo, kw & E));
+                phi = __vmaxu2((old >> 8) & E, __vminu2(dhi, (kw >> 8) & E));
+                nw = plo | (phi << 8);
+            } else {
+                uint32_t left = __shfl_up_sync(FULL, plo, 1), right = __shfl_down_sync(FULL, plo, 1);
+                if (lane == 0) left = sm.hLm[rp] << 16;
+                if (lane == 31) right = sm.hRm[rp];
+                const uint32_t dil =
+                    __vimax3_u16x2(plo, __funnelshift_l(left, plo, 16), __funnelshift_r(plo, right, 16));
+                nw = __vmaxu2(old, __vminu2(dil, kw));
+                plo = nw;
+            }
+            sm.tm[r * 32 + lane] = nw;
+            const uint32_t x = nw ^ old;
+            diff |= x;
+            if (x != 0u) chg |= 1ull << (r - 1);
+        }
+        col_now |= (diff & edge_mask) != 0u;
+        __syncwarp();
+        return warp_or64(chg);
+    }
     uint32_t prev[N];
     P::unpack(sm.tm[(DOWN ? first - 1 : first + 1) * 32 + lane], prev);
 #pragma unroll 4
@@ -566,20 +613,146 @@ __device__ __forceinline__ void hscan_rows(uint32_t (&m)[R][Px<DT>::PPW], const 
     }
 }
 
-// Horizontal pass over the rows in `rows` (in blocks of four): forward then
-// backward scan, which leaves each row at its one-dimensional fixed point.
+// Q pairs of rows scanned together in one direction, uint8 / uint16: pixel
+// j of a pair's two rows shares one word as u16x2 (first row low), so every
+// min / max, and each step of the clamp-map scan (A and B in a word each),
+// serves two rows at once.  The algebra is hscan's, element-wise.
+template <bool FWD, int Q, int N>
+__device__ __forceinline__ void hscan_pairs(uint32_t (&m)[Q][N], const uint32_t (&k)[Q][N], const uint32_t (&cin)[Q],
+                                            int lane) {
+    const int first = FWD ? 0 : N - 1, last = FWD ? N - 1 : 0;
+    const int edge_lane = FWD ? 0 : 31;
+    bool need = false;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+#pragma unroll
+        for (int s = 1; s < N; ++s) {
+            const int j = FWD ? s : N - 1 - s;
+            const int jp = FWD ? j - 1 : j + 1;
+            m[q][j] = __vmaxu2(m[q][j], __vminu2(m[q][jp], k[q][j]));
+        }
+        uint32_t in_px = FWD ? __shfl_up_sync(FULL, m[q][last], 1) : __shfl_down_sync(FULL, m[q][last], 1);
+        if (lane == edge_lane) in_px = cin[q];
+        need |= __vcmpgtu2(__vminu2(in_px, k[q][first]), m[q][first]) != 0u;
+    }
+    if (!__any_sync(FULL, need)) return;
+    uint32_t A[Q], B[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        A[q] = m[q][last];
+        B[q] = k[q][0];
+#pragma unroll
+        for (int j = 1; j < N; ++j) B[q] = __vminu2(B[q], k[q][j]);
+        if (lane == edge_lane) {
+            A[q] = __vmaxu2(A[q], __vminu2(cin[q], B[q]));
+            B[q] = 0u;  // the entry lane becomes a constant: nothing before it
+        }
+    }
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1)
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const uint32_t Ap = FWD ? __shfl_up_sync(FULL, A[q], d) : __shfl_down_sync(FULL, A[q], d);
+            const uint32_t Bp = FWD ? __shfl_up_sync(FULL, B[q], d) : __shfl_down_sync(FULL, B[q], d);
+            A[q] = __vmaxu2(__vminu2(Ap, B[q]), A[q]);
+            B[q] = __vminu2(Bp, B[q]);
+        }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        uint32_t c = FWD ? __shfl_up_sync(FULL, A[q], 1) : __shfl_down_sync(FULL, A[q], 1);
+        if (lane == edge_lane) c = cin[q];
+#pragma unroll
+        for (int s = 0; s < N; ++s) {
+            const int j = FWD ? s : N - 1 - s;
+            c = __vminu2(c, k[q][j]);
+            m[q][j] = __vmaxu2(m[q][j], c);
+        }
+    }
+}
+
+// Two row words (a: first row, b: second) as the pair words of hscan_pairs
+// and back.  uint8: pixel j of both rows from the words' even / odd bytes;
+// uint16: the words' low / high halves.
+template <int DT>
+__device__ __forceinline__ void pair_pack(uint32_t a, uint32_t b, uint32_t (&p)[Px<DT>::PPW]) {
+    if constexpr (DT == DT_U8) {
+        constexpr uint32_t E = 0x00ff00ffu;
+        const uint32_t la = a & E, ha = (a >> 8) & E, lb = b & E, hb = (b >> 8) & E;
+        p[0] = __byte_perm(la, lb, 0x5410);
+        p[1] = __byte_perm(ha, hb, 0x5410);
+        p[2] = __byte_perm(la, lb, 0x7632);
+        p[3] = __byte_perm(ha, hb, 0x7632);
+    } else {
+        p[0] = __byte_perm(a, b, 0x5410);
+        p[1] = __byte_perm(a, b, 0x7632);
+    }
+}
+template <int DT>
+__device__ __forceinline__ void pair_unpack(const uint32_t (&p)[Px<DT>::PPW], uint32_t& a, uint32_t& b) {
+    if constexpr (DT == DT_U8) {
+        const uint32_t t = __byte_perm(p[0], p[1], 0x6240), u = __byte_perm(p[2], p[3], 0x6240);
+        a = __byte_perm(t, u, 0x5410);
+        b = __byte_perm(t, u, 0x7632);
+    } else {
+        a = __byte_perm(p[0], p[1], 0x5410);
+        b = __byte_perm(p[0], p[1], 0x7632);
+    }
+}
+
+// Horizontal pass over the rows in `rows` (in blocks of eight as four row
+// pairs for uint8 / uint16, of four for int32): forward then backward scan,
+// which leaves each row at its one-dimensional fixed point.  `nrows` counts
+// the rows of the blocks processed.
 template <int DT, int TH>
 __device__ __forceinline__ unsigned long long hpass(WarpSmem<TH>& sm, int lane, unsigned long long rows,
-                                                    uint32_t edge_mask, bool& col_now, unsigned& blocks) {
+                                                    uint32_t edge_mask, bool& col_now, unsigned& nrows) {
     using P = Px<DT>;
     constexpr int N = P::PPW;
-    constexpr int R = 4;
     unsigned long long chg = 0ull;
     uint32_t diff = 0u;
+    if constexpr (DT != DT_I32) {
+        constexpr int Q = 4, R = 2 * Q;
+        static_assert(TH % R == 0, "tile rows: a multiple of 8");
+#pragma unroll 1
+        for (int b = 0; b < TH; b += R) {
+            if (((rows >> b) & ((1ull << R) - 1ull)) == 0ull) continue;
+            nrows += R;
+            uint32_t m[Q][N], k[Q][N], olda[Q], oldb[Q], cin[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const int r = b + 2 * q + 1;
+                olda[q] = sm.tm[r * 32 + lane];
+                oldb[q] = sm.tm[(r + 1) * 32 + lane];
+                pair_pack<DT>(olda[q], oldb[q], m[q]);
+                pair_pack<DT>(sm.tk[r * 32 + lane], sm.tk[(r + 1) * 32 + lane], k[q]);
+                cin[q] = sm.hLm[r] | (sm.hLm[r + 1] << 16);
+            }
+            hscan_pairs<true, Q, N>(m, k, cin, lane);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) cin[q] = sm.hRm[b + 2 * q + 1] | (sm.hRm[b + 2 * q + 2] << 16);
+            hscan_pairs<false, Q, N>(m, k, cin, lane);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const int r = b + 2 * q + 1;
+                uint32_t na, nb;
+                pair_unpack<DT>(m[q], na, nb);
+                sm.tm[r * 32 + lane] = na;
+                sm.tm[(r + 1) * 32 + lane] = nb;
+                const uint32_t xa = na ^ olda[q], xb = nb ^ oldb[q];
+                diff |= xa | xb;
+                if (xa != 0u) chg |= 1ull << (b + 2 * q);
+                if (xb != 0u) chg |= 1ull << (b + 2 * q + 1);
+            }
+        }
+        col_now |= (diff & edge_mask) != 0u;
+        __syncwarp();
+        return warp_or64(chg);
+    }
+    constexpr int R = 4;
 #pragma unroll 1
     for (int b = 0; b < TH; b += R) {
         if (((rows >> b) & ((1ull << R) - 1ull)) == 0ull) continue;
-        ++blocks;
+        nrows += R;
         uint32_t m[R][N], k[R][N], old[R], cin[R];
 #pragma unroll
         for (int q = 0; q < R; ++q) {
@@ -775,19 +948,22 @@ template <int DT>
 __device__ __forceinline__ bool pq_raise(uint32_t* words, int r, int c, uint32_t v, bool* fail) {
     using P = Px<DT>;
     uint32_t* w = &words[r * 32 + c / P::PPW];
-    if (DT == DT_I32) return atomicMax(reinterpret_cast<int*>(w), (int)v) < (int)v;
-    constexpr int B = 8 * P::BPP;
-    const int sh = B * (c % P::PPW);
-    const uint32_t msk = ((1u << B) - 1u) << sh;
-    uint32_t old = *(volatile uint32_t*)w;
-    for (int it = 0; it < 64; ++it) {
-        if (((old & msk) >> sh) >= v) return false;
-        const uint32_t got = atomicCAS(w, old, (old & ~msk) | (v << sh));
-        if (got == old) return true;
-        old = got;
+    if constexpr (DT == DT_I32) {
+        return atomicMax(reinterpret_cast<int*>(w), (int)v) < (int)v;
+    } else {
+        constexpr int B = 8 * P::BPP;
+        const int sh = B * (c % P::PPW);
+        const uint32_t msk = ((1u << B) - 1u) << sh;
+        uint32_t old = *(volatile uint32_t*)w;
+        for (int it = 0; it < 64; ++it) {
+            if (((old & msk) >> sh) >= v) return false;
+            const uint32_t got = atomicCAS(w, old, (old & ~msk) | (v << sh));
+            if (got == old) return true;
+            old = got;
+        }
+        *fail = true;
+        return false;
     }
-    *fail = true;
-    return false;
 }
 
 template <int DT, int CONN, int TH>
@@ -1112,9 +1288,7 @@ __device__ __forceinline__ VisitResult visit_tile(const ImgDesc& d, int tx, int 
                 dH |= chg;
             } else {
                 if (dH == 0ull) continue;
-                unsigned blocks = 0u;
-                chg = hpass<DT, TH>(sm, lane, dH, edge_mask, col_now, blocks);
-                res.row_steps += 4u * blocks;
+                chg = hpass<DT, TH>(sm, lane, dH, edge_mask, col_now, res.row_steps);
                 dH = 0ull;
                 dVd |= (chg << 1) & ALL;
                 dVu |= chg >> 1;
