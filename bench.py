@@ -533,7 +533,8 @@ def bench_config1(args, dev, variant, handle, tune=True):
     stream = torch.cuda.Stream(dev)
     steps = max(args.steps, 20)
     solver = getattr(args, "config1_solver", None)
-    cfg = None if solver is None else __import__("ctypes").byref(iwpp.Config.make(solver=solver))
+    tile_rows = getattr(args, "config1_tile_rows", 0)
+    cfg = None if solver is None else __import__("ctypes").byref(iwpp.Config.make(solver=solver, tile_rows=tile_rows))
 
     # the autotuner once per image class (4096^2 uint8 at each connectivity,
     # tuned on its h = 40 image); the default calls below read its table
@@ -633,7 +634,8 @@ def bench_config1(args, dev, variant, handle, tune=True):
         pipelined_step(finish=k == e2e_steps - 1)
     secs = time.perf_counter() - ts
     e2e_ok = all(np.array_equal(host_out[i].numpy(), results[i]) for i in range(len(cases)))
-    return {"workload": CONFIG1, "variant": variant, "autotuned": tuned or None, "solver": solver, "steps": steps,
+    return {"workload": CONFIG1, "variant": variant, "autotuned": tuned or None, "solver": solver,
+            "tile_rows": tile_rows if solver is not None else None, "steps": steps,
             "gpx_s": px_step * steps / (elapsed / 1e3) / 1e9,
             "inputs_sha256": inputs_sha256(mask_np, *[m for _, _, m in cases]),
             "ms_per_step": elapsed / steps, "mean_reconstruction_ms": mean_ms,
@@ -945,6 +947,8 @@ def main():
     ap.add_argument("--config1-solver", type=int, default=None, choices=[0, 1, 2, 3],
                     help="with --config1-only: every call with this in-tile solver (the configuration the "
                          "autotuner picks, without its launches before the profiled ones)")
+    ap.add_argument("--config1-tile-rows", type=int, default=0, choices=[0, 32, 64],
+                    help="with --config1-solver: the tile height as well (0: the default)")
     ap.add_argument("--profile-headline", type=int, default=0, metavar="N",
                     help="only N reconstructions of the headline image with the front stage (for profilers)")
     ap.add_argument("--profile-passes", type=int, default=2,
