@@ -556,10 +556,11 @@ __global__ void __launch_bounds__(32) sweep_y4n_kernel(ImgDesc d, uint32_t* seg_
         cp_async_wait<NG - 1>();
         __syncwarp();
         const int sb = base % NR;
-        uint32_t out[kGroup];
+        uint32_t out[kGroup], orig[kGroup];
 #pragma unroll
         for (int q = 0; q < kGroup; ++q) {
             uint32_t m = ring_m[sb + q][lane], k = ring_k[sb + q][lane];
+            orig[q] = m;
             const bool live = base + q < H;  // rows past the segment: stale slots
             if (DT == DT_U8) {
                 m = __byte_perm(m, 0u, 0x4140);
@@ -588,14 +589,17 @@ __global__ void __launch_bounds__(32) sweep_y4n_kernel(ImgDesc d, uint32_t* seg_
             }
         }
         if (MODE != 1) {
+            // only the elements that rose are stored: an unchanged store
+            // would still dirty its L2 sector and cost a DRAM write-back
             if (nbytes >= 2) {
 #pragma unroll
                 for (int q = 0; q < kGroup; ++q)
-                    if (base + q < H)
+                    if (base + q < H && out[q] != orig[q])
                         *reinterpret_cast<uint16_t*>(mo + (long long)(base + q) * step_m) = (uint16_t)out[q];
             } else if (nbytes == 1) {
                 for (int q = 0; q < kGroup; ++q)
-                    if (base + q < H) *(mo + (long long)(base + q) * step_m) = (unsigned char)out[q];
+                    if (base + q < H && (out[q] & 0xffu) != (orig[q] & 0xffu))
+                        *(mo + (long long)(base + q) * step_m) = (unsigned char)out[q];
             }
         }
         __syncwarp();
