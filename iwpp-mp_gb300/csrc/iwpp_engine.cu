@@ -475,12 +475,12 @@ __device__ int mutex_global_take(const EngineArgs& a, int lane, WarpCounters& cn
     look = __shfl_sync(FULL, look, 0);
     if (look == 2) return 1;
     if (look == 0) return 2;
-    int n = 0, base = 0, verdict = 0;  // verdict: 0 entries / nothing, 1 exit, 2 refill
+    int n = 0, base = 0, outcome = 0;  // outcome: 0 entries / nothing, 1 exit, 2 refill
     unsigned ticket = 0u;
     int top = 0;
     if (lane == 0) {
         if (!mutex_lock(a, &ticket, &top)) {
-            verdict = 1;
+            outcome = 1;
         } else {
             if (top > 0) {
                 const int want = *(volatile int*)&s_cq.waiting + 1;
@@ -493,22 +493,22 @@ __device__ int mutex_global_take(const EngineArgs& a, int lane, WarpCounters& cn
                 if (ld_volatile(&a.ctrl->overflow) != 0u) {
                     if ((int)ld_volatile(&a.ctrl->restarts) >= a.max_restarts) {
                         set_error(a.ctrl, DEV_ERR_OVERFLOW);
-                        verdict = 1;
+                        outcome = 1;
                     } else {
-                        verdict = 2;
+                        outcome = 2;
                     }
                 } else {
-                    verdict = 1;
+                    outcome = 1;
                 }
             }
-            if (n == 0 && verdict != 2) mutex_unlock(a, ticket, top);
+            if (n == 0 && outcome != 2) mutex_unlock(a, ticket, top);
         }
     }
     n = __shfl_sync(FULL, n, 0);
     base = __shfl_sync(FULL, base, 0);
-    verdict = __shfl_sync(FULL, verdict, 0);
-    if (verdict == 1) return 1;
-    if (verdict == 2) {
+    outcome = __shfl_sync(FULL, outcome, 0);
+    if (outcome == 1) return 1;
+    if (outcome == 2) {
         // quiescent with lost insertions: refill with every tile (lock held)
         for (unsigned i = (unsigned)lane; i < a.G && i < a.cap; i += 32u) a.q0[i] = a.G - 1u - i;
         __threadfence();
@@ -576,13 +576,13 @@ __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
         if (ld_volatile(&a.ctrl->error) != 0u) break;
         const long long qr0 = clock64();
         unsigned g = cta_take(a, lane);
-        int verdict = 0;  // 0 an entry, 1 exit, 2 nothing now
+        int outcome = 0;  // 0 an entry, 1 exit, 2 nothing now
         if (g == ~0u) {
             int taker = 0;
             if (lane == 0) taker = atomicCAS(&s_cq.taker, 0, 1) == 0 ? 1 : 0;
             taker = __shfl_sync(FULL, taker, 0);
             if (taker) {
-                verdict = mutex_global_take(a, lane, cnt, &g);
+                outcome = mutex_global_take(a, lane, cnt, &g);
                 __syncwarp();
                 if (lane == 0) atomicExch(&s_cq.taker, 0);
             } else {
@@ -592,11 +592,11 @@ __device__ void mutex_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
                 if (lane == 0)
                     over = ld_volatile(&a.ctrl->pending) == 0 && stack_top(a.ctrl) == 0 &&
                            ld_volatile(&a.ctrl->overflow) == 0u;
-                verdict = __shfl_sync(FULL, over, 0) ? 1 : 2;
+                outcome = __shfl_sync(FULL, over, 0) ? 1 : 2;
             }
         }
-        if (verdict == 1) break;
-        if (verdict == 2) {
+        if (outcome == 1) break;
+        if (outcome == 2) {
             // nothing to take but work in flight: back off, bounded by progress
             if (!idle) {
                 if (lane == 0) {
@@ -667,7 +667,7 @@ __device__ void async_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
         p = __shfl_sync(FULL, p, 0);
         unsigned g = a.init_list && p < n0 ? __ldcg(&a.init_list[p]) : p;
         if (p >= n0) {
-            int verdict = 0;  // 0 got an entry, 1 exit
+            int outcome = 0;  // 0 got an entry, 1 exit
             unsigned v = 0u;
             if (lane == 0) {
                 const unsigned slot = (p - n0) % a.cap;
@@ -684,7 +684,7 @@ __device__ void async_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
                     // the job's counters every eighth look
                     if ((++spins & 7u) == 0u) {
                         if (ld_volatile(&a.ctrl->pending) == 0 || ld_volatile(&a.ctrl->error) != 0u) {
-                            verdict = 1;
+                            outcome = 1;
                             break;
                         }
                         const unsigned prog = ld_volatile(&a.ctrl->progress);
@@ -694,7 +694,7 @@ __device__ void async_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
                             idle_since = now;
                         } else if (now - idle_since > a.timeout_ns) {
                             set_error(a.ctrl, DEV_ERR_TIMEOUT);
-                            verdict = 1;
+                            outcome = 1;
                             break;
                         }
                     }
@@ -702,9 +702,9 @@ __device__ void async_worker(const EngineArgs& a, WarpSmem<TH>& sm, int lane, Wa
                     if (ns < 256) ns <<= 1;
                 }
             }
-            verdict = __shfl_sync(FULL, verdict, 0);
+            outcome = __shfl_sync(FULL, outcome, 0);
             cnt.phase[0] += clock64() - qr0;
-            if (verdict) return;
+            if (outcome) return;
             g = __shfl_sync(FULL, v, 0) - 1u;
         } else {
             cnt.phase[0] += clock64() - qr0;
