@@ -65,7 +65,8 @@ typedef struct iwpp_config {
                                   (mutex queue: always 64) */
     long long queue_capacity;  /* entries per queue buffer; 0 = default; < 0: that multiple
                                   of the job's tile count */
-    int init_passes;           /* whole-image passes first (+X, +Y, -X, -Y each); -1 = default (0) */
+    int init_passes;           /* whole-image passes first (+X, +Y, -X, -Y each); -1 = default
+                                  (0; 2 inside the front stage) */
     int grid_ctas;             /* persistent grid size; 0 = one full wave */
     int max_restarts;          /* queue-overflow restarts allowed; 0 = default (64) */
     int timeout_ms;            /* bound on every device-side wait; 0 = default (10000) */
