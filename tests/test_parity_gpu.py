@@ -87,6 +87,29 @@ def test_random_shapes(dt, conn, variant):
 
 @pytest.mark.parametrize("dt", [0, 1, 2])
 @pytest.mark.parametrize("conn", [4, 8])
+@pytest.mark.parametrize("variant", ["async", "unique"])
+def test_pass_solver(dt, conn, variant):
+    # solver 2: every visit by vertical / horizontal passes (packed-word
+    # vertical chains, paired-row horizontal scans for uint8 / uint16), first
+    # visits with every row dirty, revisits from the sides that rose; ragged
+    # shapes (rows past the image inside a tile), both tile heights
+    rng = np.random.default_rng(500 + 10 * dt + conn + len(variant))
+    shapes = [(1, 1), (3, 5), (37, 53), (65, 129), (200, 333), (513, 257), (700, 1500)]
+    for i, (h, w) in enumerate(shapes):
+        mask = synth.noise_mask(w, h, dt, 90 + i, 2.0 + i, 3 + 2 * i)
+        if i % 3 == 0:
+            marker = synth.sparse_marker(mask, 27 + i, 0.002)
+        else:
+            marker = synth.hdome_marker(mask, int(rng.integers(5, 120)))
+        ref = oracle.reconstruct(marker, mask, conn)
+        for th in (32, 64):
+            out, st = gpu_reconstruct(marker, mask, conn, variant, iwpp.Config.make(solver=2, tile_rows=th))
+            assert st.status == 0
+            assert np.array_equal(out, ref), (h, w, th, int((out != ref).sum()))
+
+
+@pytest.mark.parametrize("dt", [0, 1, 2])
+@pytest.mark.parametrize("conn", [4, 8])
 @pytest.mark.parametrize("variant", VARIANTS)
 def test_pixel_queue_solver(dt, conn, variant):
     # solver 3: revisits by the per-tile pixel queue (first visits by passes);
